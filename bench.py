@@ -1,0 +1,361 @@
+"""Benchmark of the hot path: MLUPS and the HBM roofline of the fused LBM sweep.
+
+Workload (default): D3Q27 BGK flow past a spanwise cylinder on a 512x128x128
+grid (D = 32 cells, axis along z through (128, 64)), equilibrium inlet
+u = (0.04, 0, 0), zero-gradient outlet, free-slip y, periodic z, Re = 200
+(tau = 0.5 + 3 u D / Re = 0.5192), initial rho = 1, uniform u plus a seeded
++-1e-3 u_y perturbation.  Populations are stored in FP64; the collision is
+computed in FP32 (the FP64-storage form of the precision study; GB300's FP64
+units run at ~1 TFLOP/s, which makes FP64 arithmetic ALU-bound -- that variant
+is measured and reported alongside as "fp64_arith").
+
+One step = one time step of the whole grid (boundary kernel + fused sweep).
+`value` = interior cells x timed steps / device time (MLUPS), inputs resident;
+`e2e` = the same metric through the C ABI end to end: create the handle from
+host buffers, step, read every step's force (Cd, Cl) back to the host as the
+reference's test.dat loop does, and read the final u, v, w, p fields back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cylinder-flow_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+NX, NY, NZ = 512, 128, 128
+D, U_IN, RE = 32.0, 0.04, 200.0
+TAU0 = 3.0 * U_IN * D / RE           # reference System::tau; tau = tau0 + 0.5
+WORKLOAD = dict(lattice=27, nx=NX, ny=NY, nz=NZ, tau0=TAU0, u0=U_IN, wall_y="freeslip",
+                wall_z="periodic", geom="cylinder", cx=128.0, cy=64.0, diam=D,
+                perturb_amp=1e-3, seed=1234)
+CELLS = NX * NY * NZ
+METRIC = "MLUPS (D3Q27 BGK sweep, 512x128x128 spanwise cylinder)"
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            m = json.load(fh)
+        return float(m["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the sweep from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "sweep_d3q27_512x128x128.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if r[4 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def time_device(solver, steps, warmup):
+    """Device time of `steps` steps on the solver's stream (CUDA events)."""
+    import torch
+    stream = torch.cuda.ExternalStream(solver.stream_ptr())
+    solver.step(warmup)
+    solver.synchronize()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)  # ms
+
+
+def variant_mlups(cflbm, local, storage, compute, steps, warmup):
+    with cflbm.Solver(device=local, storage=storage, compute=compute, **WORKLOAD) as s:
+        ms = time_device(s, steps, warmup)
+        s.set_timing(True)
+        s.step(max(steps // 4, 3))
+        sw_ms, bd_ms, n_sw, n_bd = s.timing()
+        info = s.info()
+    return {"mlups": CELLS * steps / (ms * 1e-3) / 1e6,
+            "sweep_us": 1e3 * sw_ms / max(n_sw, 1),
+            "boundary_us": 1e3 * bd_ms / max(n_bd, 1),
+            "bytes_per_cell": info.bytes_per_cell_step}
+
+
+def run_gb300(args):
+    world, rank, local = dist_setup(args)
+    import torch
+    import cflbm
+
+    peak, peak_kind = peaks()
+    steps, warmup = args.steps, args.warmup
+    launches0 = cflbm.launch_count()
+    # ---- device-resident timing of the headline variant -------------------------
+    with cflbm.Solver(device=local, storage="fp64", compute="fp32", **WORKLOAD) as s:
+        stream = torch.cuda.ExternalStream(s.stream_ptr())
+        s.step(warmup)
+        s.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            n_launch0 = cflbm.launch_count()
+            e0.record(stream)
+            s.step(steps)
+            e1.record(stream)
+            e1.synchronize()
+            n_launch = cflbm.launch_count() - n_launch0
+        torch.cuda.synchronize()
+        barrier(world)
+        ms = max_over_ranks(e0.elapsed_time(e1), world)
+        # Per-kernel timing of the sweep (events around each launch, same stream).
+        s.set_timing(True)
+        s.step(max(steps // 2, 3))
+        sw_ms, bd_ms, n_sw, n_bd = s.timing()
+        s.set_timing(False)
+        info = s.info()
+        f, cdcl = s.forces()
+        mass, _ = s.mass()
+    value = world * CELLS * steps / (ms * 1e-3) / 1e6
+    sweep_s = sw_ms * 1e-3 / max(n_sw, 1)
+    achieved = info.bytes_per_cell_step * CELLS / sweep_s / 1e9
+    traffic = profile_traffic()
+
+    # ---- the other storage/arithmetic forms at the same grid ---------------------
+    extra = {}
+    if not args.quick:
+        for name, st, cp in (("fp64_arith", "fp64", "fp64"), ("fp32_store", "fp32", "fp32"),
+                             ("fp16dev_store", "fp16dev", "fp32")):
+            v = variant_mlups(cflbm, local, st, cp, max(steps // 3, 20) if cp == "fp64" else steps,
+                              min(warmup, 5))
+            v["hbm_frac"] = v["bytes_per_cell"] * CELLS / (v["sweep_us"] * 1e-6) / 1e9 / peak
+            extra[name] = {k: round(x, 4) if isinstance(x, float) else x for k, x in v.items()}
+
+    # ---- end to end through the C ABI with host buffers --------------------------
+    e2e_steps = max(steps // 2, 10)
+    solid = np.zeros((NZ, NY, NX), np.uint8)
+    yy, xx = np.mgrid[0:NY, 0:NX]
+    solid[:, ((xx - 128.0) ** 2 + (yy - 64.0) ** 2) <= (D / 2) ** 2] = 1
+    pinned = [torch.empty((NZ, NY, NX), dtype=torch.float64).pin_memory() for _ in range(4)]
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    wl = dict(WORKLOAD)
+    wl["geom"] = "none"
+    with cflbm.Solver(device=local, storage="fp64", compute="fp32", solid=solid, **wl) as s:
+        for _ in range(e2e_steps):
+            s.step(1)
+            s.forces()  # per-step Cd/Cl read back (reference: test.dat every step)
+        outs = [t.numpy() for t in pinned]
+        cflbm._lib.check(cflbm._lib.lib.cflbm_macros(
+            s._h, *[o.ctypes.data_as(cflbm.solver.ctypes.POINTER(cflbm.solver.ctypes.c_double))
+                    for o in outs]), "cflbm_macros")
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(t1 - t0, world)
+    e2e_value = world * CELLS * e2e_steps / e2e_s / 1e6
+    h2d = solid.nbytes / e2e_steps
+    d2h = (e2e_steps * 3 * 8 + 4 * CELLS * 8) / e2e_steps
+    gpu_launches = n_launch
+
+    # ---- CPU baseline: the reference's algorithm (oracle port), bounded sample ---
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_steps)
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": round(ms / steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded perturbation; no dataset)",
+        "config": {"workload": "D3Q27 512x128x128 spanwise cylinder D=32, Re=200, "
+                               "free-slip y, periodic z (BASELINE configs[1])",
+                   "storage": "f64", "collision": "f32", "global_cells": CELLS * world,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "working set 2 x 3.8 GB >> 129 MB L2 (no flush needed)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "bytes_per_cell": info.bytes_per_cell_step,
+                     "sweep_us": round(sweep_s * 1e6, 2),
+                     "boundary_us": round(1e3 * bd_ms / max(n_bd, 1), 2)},
+        "e2e": {"value": round(e2e_value, 2), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+        "gpu_launches": gpu_launches,
+        "clocks": clk.summary(),
+        "forms": extra,
+        "check": {"cd": cdcl[0], "cl": cdcl[1], "mass": mass, "finite": bool(np.isfinite(mass))},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def cpu_baseline(steps: int):
+    """The reference's algorithm on the host cores: the oracle port of the 3-D
+    reference solver (same passes, same serial Update loop) at 512x128x128,
+    OpenMP over all cores, timed over a bounded number of steps."""
+    from oracle import oracle as O
+    import ctypes
+    cores = os.cpu_count() or 1
+    L = O.lib()
+    lx, ly, lz = NX + 6, NY + 6, NZ + 6
+    ran = np.zeros(lx * ly * lz, np.int32)
+    t0 = time.perf_counter()
+    rc = L.oracle_ref3d_run(NX, NY, NZ, TAU0, U_IN, ran.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                            0, None, None, None, None, None, None, cores)
+    t_init = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rc |= L.oracle_ref3d_run(NX, NY, NZ, TAU0, U_IN, ran.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                             steps, None, None, None, None, None, None, cores)
+    t_run = time.perf_counter() - t0 - t_init
+    assert rc == 0
+    return {"value": round(CELLS * steps / max(t_run, 1e-9) / 1e6, 3), "unit": "MLUPS",
+            "cores": cores, "kind": "port",
+            "sample": f"{steps} steps of the 512x128x128 D3Q27 grid (reference solver "
+                      f"structure incl. its serial Update loop), init excluded"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    runs = []
+    for _ in range(max(args.steps_ref, 1)):
+        runs.append(cpu_baseline(args.cpu_steps))
+    v = statistics.median(r["value"] for r in runs)
+    cb = dict(runs[0])
+    cb["value"] = v
+    line = {
+        "metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": world, "steps": args.steps_ref,
+        "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "D3Q27 512x128x128 (reference solver on the host cores)"},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline variant only")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.steps_ref = 1
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,654 @@
+// C ABI of the solver (include/cflbm.h): handle life cycle and the step loop.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+#include "handle.hpp"
+
+using namespace cflbm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CK_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(CFLBM_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                  \
+  } while (0)
+
+int dev_alloc(cflbm_handle *h, void **p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(CFLBM_E_NOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  h->device_bytes += bytes;
+  return CFLBM_OK;
+}
+
+template <class T>
+int dev_alloc_t(cflbm_handle *h, T **p, size_t count) {
+  void *v = nullptr;
+  int rc = dev_alloc(h, &v, count * sizeof(T));
+  *p = static_cast<T *>(v);
+  return rc;
+}
+
+void free_handle(cflbm_handle *h) {
+  if (!h) return;
+  if (h->cfg.device >= 0) cudaSetDevice(h->cfg.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
+                  h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
+                  h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int store_size(int storage) {
+  return storage == CFLBM_STORE_FP64 ? 8 : storage == CFLBM_STORE_FP32 ? 4 : 2;
+}
+
+// Pack a host uint8 mask (x fastest) into 32-bit words per row.
+std::vector<uint32_t> pack_mask(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
+                                int nxw) {
+  std::vector<uint32_t> w((size_t)nxw * ny * nz, 0u);
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x)
+        if (solid[((size_t)z * ny + y) * nx + x])
+          w[((size_t)z * ny + y) * nxw + (x >> 5)] |= (1u << (x & 31));
+  return w;
+}
+
+template <int Q>
+void build_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
+                 std::vector<int4> &links, long long &n_solid) {
+  using L = Lat<Q>;
+  links.clear();
+  n_solid = 0;
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        if (!solid[((size_t)z * ny + y) * nx + x]) continue;
+        ++n_solid;
+        for (int k = 1; k < Q; ++k) {
+          const int X = x + L::ex(k), Y = y + L::ey(k), Z = z + L::ez(k);
+          if (X < 0 || X >= nx || Y < 0 || Y >= ny || Z < 0 || Z >= nz) continue;
+          if (solid[((size_t)Z * ny + Y) * nx + X]) continue;
+          links.push_back(make_int4(x, y, z, k));
+        }
+      }
+}
+
+// Equilibrium of the channel inlet (p = 0, u = (u_in, 0, 0)) in storage format.
+template <int Q>
+std::vector<unsigned char> inlet_elements(double u_in, int storage) {
+  using L = Lat<Q>;
+  std::vector<unsigned char> out((size_t)Q * store_size(storage));
+  for (int i = 0; i < Q; ++i) {
+    const double edu = L::ex(i) * u_in;
+    const double feq = L::w(i) * 0.0 * 3.0 + L::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * u_in * u_in);
+    if (storage == CFLBM_STORE_FP64) {
+      std::memcpy(&out[8 * i], &feq, 8);
+    } else if (storage == CFLBM_STORE_FP32) {
+      const float v = (float)feq;
+      std::memcpy(&out[4 * i], &v, 4);
+    } else {
+      const __half v = __float2half_rn((float)(feq * (double)L::h_scale(i)));
+      std::memcpy(&out[2 * i], &v, 2);
+    }
+  }
+  return out;
+}
+
+int validate(const cflbm_config *c) {
+  if (!c) return fail(CFLBM_E_INVALID, "config is NULL");
+  if (c->lattice != CFLBM_D2Q9 && c->lattice != CFLBM_D3Q27)
+    return fail(CFLBM_E_INVALID, "lattice must be 9 or 27, got %d", c->lattice);
+  const int nz = c->lattice == CFLBM_D2Q9 ? 1 : c->nz;
+  if (c->nx < 4 || c->ny < 4 || nz < 1 || (c->lattice == CFLBM_D3Q27 && nz < 4))
+    return fail(CFLBM_E_INVALID, "grid %dx%dx%d too small", c->nx, c->ny, nz);
+  if ((long long)c->nx * c->ny * nz > (1LL << 31))
+    return fail(CFLBM_E_INVALID, "grid of %lld cells exceeds 2^31",
+                (long long)c->nx * c->ny * nz);
+  if (c->ny > 65535 * 4 || nz > 65535)
+    return fail(CFLBM_E_INVALID, "ny or nz exceeds the launch grid limit");
+  if (c->storage < 0 || c->storage > 2)
+    return fail(CFLBM_E_INVALID, "storage %d unknown", c->storage);
+  if (c->compute < 0 || c->compute > 1)
+    return fail(CFLBM_E_INVALID, "compute %d unknown", c->compute);
+  if (c->profile < 0 || c->profile > 2)
+    return fail(CFLBM_E_INVALID, "profile %d unknown", c->profile);
+  if (c->profile == CFLBM_PROFILE_REF2D && c->lattice != CFLBM_D2Q9)
+    return fail(CFLBM_E_INVALID, "REF2D profile needs the D2Q9 lattice");
+  if (c->profile == CFLBM_PROFILE_REF3D && c->lattice != CFLBM_D3Q27)
+    return fail(CFLBM_E_INVALID, "REF3D profile needs the D3Q27 lattice");
+  if (c->wall_y < 0 || c->wall_y > 2 || c->wall_z < 0 || c->wall_z > 2)
+    return fail(CFLBM_E_INVALID, "wall type out of range");
+  if (!(c->tau0 > -0.5 + 1e-9) || !std::isfinite(c->tau0))
+    return fail(CFLBM_E_INVALID, "tau0 = %g gives omega outside (0, 2)", c->tau0);
+  if (!std::isfinite(c->u0)) return fail(CFLBM_E_INVALID, "u0 is not finite");
+  if (c->force_history < 0) return fail(CFLBM_E_INVALID, "force_history < 0");
+  return CFLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cflbm_last_error(void) { return g_last_error.c_str(); }
+
+int64_t cflbm_launch_count(void) { return (int64_t)launches(); }
+
+int cflbm_config_default(cflbm_config *c) {
+  if (!c) return fail(CFLBM_E_INVALID, "config is NULL");
+  std::memset(c, 0, sizeof(*c));
+  c->lattice = CFLBM_D2Q9;
+  c->nx = 64;
+  c->ny = 32;
+  c->nz = 1;
+  c->storage = CFLBM_STORE_FP64;
+  c->compute = CFLBM_COMPUTE_FP64;
+  c->profile = CFLBM_PROFILE_CHANNEL;
+  c->wall_y = CFLBM_WALL_FREESLIP;
+  c->wall_z = CFLBM_WALL_PERIODIC;
+  c->tau0 = 0.03;
+  c->u0 = 0.05;
+  c->geom = CFLBM_GEOM_NONE;
+  c->seed = 1234;
+  return CFLBM_OK;
+}
+
+int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
+  if (!out) return fail(CFLBM_E_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  std::unique_ptr<cflbm_handle, void (*)(cflbm_handle *)> hp(new cflbm_handle(), free_handle);
+  cflbm_handle *h = hp.get();
+  h->cfg = *cfg;
+  h->cfg.solid = nullptr;
+  h->cfg.alpha = nullptr;
+  h->cfg.ref_ran = nullptr;
+  h->Q = cfg->lattice;
+  const int Q = h->Q;
+  const bool d3 = Q == 27;
+  const int nx = cfg->nx, ny = cfg->ny, nz = d3 ? cfg->nz : 1;
+  h->cfg.nz = nz;
+  CK_CUDA(cudaSetDevice(cfg->device));
+  CK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+
+  // Layout: ghosts as the profile needs them (the reference's 2 or 3 layers,
+  // 1 for the channel), rows padded to 128 bytes with >= 4 spare elements past
+  // the last ghost (the reference's wall pass reads two cells beyond the ring).
+  const int es = store_size(cfg->storage);
+  h->esize = es;
+  const int G = cfg->profile == CFLBM_PROFILE_CHANNEL ? 1 : (cfg->profile == CFLBM_PROFILE_REF2D ? 2 : 3);
+  const int align = 128 / es;
+  Layout &L = h->L;
+  L.nx = nx;
+  L.ny = ny;
+  L.nz = nz;
+  L.G = G;
+  L.Gz = d3 ? G : 0;
+  L.xoff = align;
+  L.px = ((align + nx + G + 4 + align - 1) / align) * align;
+  L.nyp = ny + 2 * G;
+  L.nzp = nz + 2 * L.Gz;
+  L.S = (long long)L.px * L.nyp * L.nzp;
+  h->nxw = (nx + 31) / 32;
+  h->omega = 1.0 / (cfg->tau0 + 0.5);
+  if (!(h->omega > 0.0 && h->omega < 2.0))
+    return fail(CFLBM_E_INVALID, "omega = %g outside (0, 2)", h->omega);
+
+  // Host-side geometry and initial fields.
+  std::vector<uint8_t> solid;
+  RefSetup ref;
+  if (cfg->profile == CFLBM_PROFILE_REF2D) {
+    ref2d_setup(nx, ny, cfg->u0, cfg->ref_ran, ref);
+    solid = ref.solid;
+    h->area = ref.area;
+  } else if (cfg->profile == CFLBM_PROFILE_REF3D) {
+    ref3d_setup(nx, ny, nz, cfg->u0, cfg->ref_ran, ref);
+    solid = ref.solid;
+    h->area = ref.area;
+  } else {
+    channel_mask(h->cfg, solid);
+    if (cfg->solid) {
+      for (size_t n = 0; n < solid.size(); ++n) solid[n] = cfg->solid[n] ? 1 : 0;
+    }
+    h->area = channel_area(h->cfg);
+  }
+  std::vector<int4> links;
+  if (d3) build_links<27>(solid, nx, ny, nz, links, h->n_solid);
+  else build_links<9>(solid, nx, ny, nz, links, h->n_solid);
+  h->n_links = (long long)links.size();
+  const std::vector<uint32_t> mask = pack_mask(solid, nx, ny, nz, h->nxw);
+
+  // Device allocations.
+  const size_t N = (size_t)nx * ny * nz;
+  h->f_bytes = (size_t)Q * L.S * es;
+  if ((rc = dev_alloc(h, &h->fA, h->f_bytes))) return rc;
+  if ((rc = dev_alloc(h, &h->fB, h->f_bytes))) return rc;
+  CK_CUDA(cudaMemsetAsync(h->fA, 0, h->f_bytes, h->stream));
+  CK_CUDA(cudaMemsetAsync(h->fB, 0, h->f_bytes, h->stream));
+  if ((rc = dev_alloc_t(h, &h->d_mask, mask.size()))) return rc;
+  CK_CUDA(cudaMemcpyAsync(h->d_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if ((rc = dev_alloc_t(h, &h->d_links, links.size() + 1))) return rc;
+  if (!links.empty())
+    CK_CUDA(cudaMemcpyAsync(h->d_links, links.data(), links.size() * sizeof(int4),
+                            cudaMemcpyHostToDevice, h->stream));
+  if ((rc = dev_alloc_t(h, &h->d_mu, N))) return rc;
+  if ((rc = dev_alloc_t(h, &h->d_mv, N))) return rc;
+  if ((rc = dev_alloc_t(h, &h->d_mw, N))) return rc;
+  if ((rc = dev_alloc_t(h, &h->d_mp, N))) return rc;
+  h->hist_cap = cfg->force_history > 0 ? cfg->force_history : 65536;
+  if ((rc = dev_alloc_t(h, &h->d_hist, 3 * (size_t)h->hist_cap))) return rc;
+  CK_CUDA(cudaMemsetAsync(h->d_hist, 0, 3 * sizeof(double) * h->hist_cap, h->stream));
+  if ((rc = dev_alloc_t(h, &h->d_step, 1))) return rc;
+  CK_CUDA(cudaMemsetAsync(h->d_step, 0, sizeof(long long), h->stream));
+  h->link_blocks = (int)std::min<long long>(std::max<long long>((h->n_links + 255) / 256, 1), 1024);
+  h->reduce_blocks = (int)std::min<long long>(std::max<long long>(((long long)N + 255) / 256, 1), 2048);
+  if ((rc = dev_alloc_t(h, &h->d_partials, 4 * (size_t)std::max(h->link_blocks, h->reduce_blocks))))
+    return rc;
+  if ((rc = dev_alloc_t(h, &h->d_counter, 1))) return rc;
+  if ((rc = dev_alloc_t(h, &h->d_counter2, 1))) return rc;
+  CK_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(unsigned), h->stream));
+  CK_CUDA(cudaMemsetAsync(h->d_counter2, 0, sizeof(unsigned), h->stream));
+  if ((rc = dev_alloc_t(h, &h->d_sums, 4))) return rc;
+
+  if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
+    std::vector<unsigned char> fin = d3 ? inlet_elements<27>(cfg->u0, cfg->storage)
+                                        : inlet_elements<9>(cfg->u0, cfg->storage);
+    if ((rc = dev_alloc(h, &h->d_fin, fin.size()))) return rc;
+    CK_CUDA(cudaMemcpyAsync(h->d_fin, fin.data(), fin.size(), cudaMemcpyHostToDevice, h->stream));
+    if (cfg->alpha) {
+      std::vector<float> a(N);
+      for (size_t n = 0; n < N; ++n) a[n] = (float)cfg->alpha[n];
+      if ((rc = dev_alloc_t(h, &h->d_alpha, N))) return rc;
+      CK_CUDA(cudaMemcpyAsync(h->d_alpha, a.data(), N * 4, cudaMemcpyHostToDevice, h->stream));
+      CK_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    CK_CUDA(launch_init_channel(Q, cfg->storage, L, h->fA, h->d_mask, h->nxw, cfg->u0,
+                                cfg->perturb_amp, cfg->seed, h->d_mu, h->d_mv, h->d_mw,
+                                h->d_mp, h->stream));
+  } else {
+    if ((rc = dev_alloc_t(h, &h->d_inlet, ref.inlet.size()))) return rc;
+    CK_CUDA(cudaMemcpyAsync(h->d_inlet, ref.inlet.data(), ref.inlet.size() * 8,
+                            cudaMemcpyHostToDevice, h->stream));
+    const size_t P = ref.u.size();
+    double *du = nullptr, *dv = nullptr, *dw = nullptr, *dp = nullptr;
+    CK_CUDA(cudaMalloc(&du, 4 * P * sizeof(double)));
+    dv = du + P;
+    dw = dv + P;
+    dp = dw + P;
+    cudaMemcpyAsync(du, ref.u.data(), P * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(dv, ref.v.data(), P * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(dw, ref.w.data(), P * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(dp, ref.p.data(), P * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaError_t e = launch_init_macros(Q, cfg->storage, L, h->fA, du, dv, dw, dp, h->stream);
+    // Step-0 macroscopic fields: the interior of the initial fields.
+    std::vector<double> mu(N), mv(N), mw(N), mp(N);
+    const int lxp = nx + 2 * G, lyp = ny + 2 * G;
+    for (int z = 0; z < nz; ++z)
+      for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+          const size_t d = ((size_t)(z + L.Gz) * lyp + (y + G)) * lxp + (x + G);
+          const size_t n = ((size_t)z * ny + y) * nx + x;
+          mu[n] = ref.u[d];
+          mv[n] = ref.v[d];
+          mw[n] = ref.w[d];
+          mp[n] = ref.p[d];
+        }
+    cudaMemcpyAsync(h->d_mu, mu.data(), N * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(h->d_mv, mv.data(), N * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(h->d_mw, mw.data(), N * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(h->d_mp, mp.data(), N * 8, cudaMemcpyHostToDevice, h->stream);
+    cudaError_t e2 = cudaStreamSynchronize(h->stream);
+    cudaFree(du);
+    CK_CUDA(e);
+    CK_CUDA(e2);
+  }
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  CK_CUDA(cudaGetLastError());
+  *out = hp.release();
+  return CFLBM_OK;
+}
+
+int cflbm_destroy(cflbm_handle *h) {
+  free_handle(h);
+  return CFLBM_OK;
+}
+
+// Record a timing event on the handle's stream (pool grows on demand).
+static int record_event(cflbm_handle *h, size_t *idx) {
+  if (h->ev_used == h->ev_pool.size()) {
+    cudaEvent_t e;
+    CK_CUDA(cudaEventCreate(&e));
+    h->ev_pool.push_back(e);
+  }
+  *idx = h->ev_used++;
+  CK_CUDA(cudaEventRecord(h->ev_pool[*idx], h->stream));
+  return CFLBM_OK;
+}
+
+static int one_step(cflbm_handle *h, bool write_macros) {
+  size_t tb0 = 0, tb1 = 0, ts0 = 0, ts1 = 0;
+  int trc;
+  if (h->timing && (trc = record_event(h, &tb0))) return trc;
+  const int Q = h->Q;
+  const int st = h->cfg.storage;
+  const Layout &L = h->L;
+  FillArgs fa{};
+  fa.L = L;
+  fa.f = h->fA;
+  fa.mask = h->d_mask;
+  fa.nxw = h->nxw;
+  fa.wall_y = h->cfg.wall_y;
+  fa.wall_z = h->cfg.wall_z;
+  fa.f_in = h->d_fin;
+  const bool ref = h->cfg.profile != CFLBM_PROFILE_CHANNEL;
+  if (!ref) {
+    CK_CUDA(launch_fill_channel(Q, st, fa, h->stream));
+  } else if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
+    // "MPI Kokkos/lbm.cpp:315-345": inlet, outlet, then the two wall rows.
+    const FaceOp ops[4] = {{0, 0, 0}, {1, 0, 1}, {2, 1, 0}, {2, 1, 1}};
+    for (const FaceOp &op : ops) CK_CUDA(launch_face_op(Q, st, fa, op, h->stream));
+  } else {
+    // "3D MPI+KOKKOS+MPIIO/lbm.cpp:278-347": front, back, bottom, top, inlet, outlet.
+    const FaceOp ops[6] = {{2, 1, 0}, {2, 1, 1}, {2, 2, 0}, {2, 2, 1}, {0, 0, 0}, {1, 0, 1}};
+    for (const FaceOp &op : ops) CK_CUDA(launch_face_op(Q, st, fa, op, h->stream));
+  }
+  LinkArgs la{};
+  la.L = L;
+  la.f = h->fA;
+  la.links = h->d_links;
+  la.n = h->n_links;
+  la.reach = ref ? 2 : 1;
+  la.partials = h->d_partials;
+  la.counter = h->d_counter;
+  la.hist = h->d_hist;
+  la.step = h->d_step;
+  la.cap = h->hist_cap;
+  CK_CUDA(launch_links(Q, st, la, h->link_blocks, h->stream));
+  if (h->timing) {
+    if ((trc = record_event(h, &tb1))) return trc;
+    h->bnd_ev.push_back({tb0, tb1});
+    if ((trc = record_event(h, &ts0))) return trc;
+  }
+  SweepArgs sa{};
+  sa.L = L;
+  sa.fa = h->fA;
+  sa.fb = h->fB;
+  sa.mask = h->d_mask;
+  sa.nxw = h->nxw;
+  sa.omega = h->omega;
+  sa.omega_f = (float)h->omega;
+  sa.ref_override = ref ? 1 : 0;
+  sa.inlet_u = h->d_inlet;
+  sa.alpha = h->d_alpha;
+  if (write_macros) {
+    sa.mu = h->d_mu;
+    sa.mv = h->d_mv;
+    sa.mw = h->d_mw;
+    sa.mp = h->d_mp;
+  }
+  CK_CUDA(launch_sweep(Q, st, h->cfg.compute, sa, h->stream));
+  if (h->timing) {
+    if ((trc = record_event(h, &ts1))) return trc;
+    h->sweep_ev.push_back({ts0, ts1});
+  }
+  if (ref) CK_CUDA(launch_ghost_copy(Q, st, L, h->fA, h->fB, h->stream));
+  std::swap(h->fA, h->fB);
+  ++h->steps_done;
+  return CFLBM_OK;
+}
+
+int cflbm_step(cflbm_handle *h, int nsteps) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  if (nsteps < 0) return fail(CFLBM_E_INVALID, "nsteps < 0");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = one_step(h, s == nsteps - 1);
+    if (rc) return rc;
+  }
+  return CFLBM_OK;
+}
+
+int cflbm_synchronize(cflbm_handle *h) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  CK_CUDA(cudaGetLastError());
+  return CFLBM_OK;
+}
+
+int cflbm_macros(cflbm_handle *h, double *u, double *v, double *w, double *p) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t N = (size_t)h->L.nx * h->L.ny * h->L.nz;
+  double *dst[4] = {u, v, w, p};
+  double *src[4] = {h->d_mu, h->d_mv, h->d_mw, h->d_mp};
+  for (int k = 0; k < 4; ++k)
+    if (dst[k]) CK_CUDA(cudaMemcpyAsync(dst[k], src[k], N * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  return CFLBM_OK;
+}
+
+int cflbm_macros_device(cflbm_handle *h, double *u, double *v, double *w, double *p) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t N = (size_t)h->L.nx * h->L.ny * h->L.nz;
+  double *dst[4] = {u, v, w, p};
+  double *src[4] = {h->d_mu, h->d_mv, h->d_mw, h->d_mp};
+  for (int k = 0; k < 4; ++k)
+    if (dst[k]) CK_CUDA(cudaMemcpyAsync(dst[k], src[k], N * 8, cudaMemcpyDeviceToDevice, h->stream));
+  return CFLBM_OK;
+}
+
+int cflbm_forces(cflbm_handle *h, double fxyz[3], double cd_cl[2]) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  double F[3] = {0.0, 0.0, 0.0};
+  if (h->steps_done > 0) {
+    const long long slot = (h->steps_done - 1) % h->hist_cap;
+    CK_CUDA(cudaMemcpyAsync(F, h->d_hist + 3 * slot, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            h->stream));
+  }
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  if (fxyz) {
+    fxyz[0] = F[0];
+    fxyz[1] = F[1];
+    fxyz[2] = F[2];
+  }
+  if (cd_cl) {
+    const double u0 = h->cfg.u0;
+    if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
+      // The reference's own expression ("MPI Kokkos/lbm.cpp:404").
+      cd_cl[0] = 2.0 * F[0] / u0 / u0 / 0.03125 / (h->L.nx - 1);
+      cd_cl[1] = 2.0 * F[1] / u0 / u0 / 0.03125 / (h->L.nx - 1);
+    } else {
+      cd_cl[0] = 2.0 * F[0] / (u0 * u0 * h->area);
+      cd_cl[1] = 2.0 * F[1] / (u0 * u0 * h->area);
+    }
+  }
+  return CFLBM_OK;
+}
+
+int cflbm_force_history(cflbm_handle *h, double *out, int64_t max_steps, int64_t *n_out) {
+  if (!h || !out || max_steps < 0) return fail(CFLBM_E_INVALID, "bad arguments");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const long long have = std::min<long long>(h->steps_done, h->hist_cap);
+  const long long n = std::min<long long>(have, max_steps);
+  // Oldest kept step first.
+  const long long first = h->steps_done - n;
+  for (long long k = 0; k < n;) {
+    const long long slot = (first + k) % h->hist_cap;
+    const long long run = std::min<long long>(n - k, h->hist_cap - slot);
+    CK_CUDA(cudaMemcpyAsync(out + 3 * k, h->d_hist + 3 * slot, run * 3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, h->stream));
+    k += run;
+  }
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  if (n_out) *n_out = n;
+  return CFLBM_OK;
+}
+
+int cflbm_mass(cflbm_handle *h, double *mass, double momentum[3]) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  ReduceArgs ra{};
+  ra.L = h->L;
+  ra.f = h->fA;
+  ra.mask = h->d_mask;
+  ra.nxw = h->nxw;
+  ra.partials = h->d_partials;
+  ra.counter = h->d_counter2;
+  ra.out = h->d_sums;
+  CK_CUDA(launch_reduce_mass(h->Q, h->cfg.storage, ra, h->reduce_blocks, h->stream));
+  double s[4];
+  CK_CUDA(cudaMemcpyAsync(s, h->d_sums, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  if (!std::isfinite(s[0])) return fail(CFLBM_E_NUMERIC, "mass is not finite (%g)", s[0]);
+  if (mass) *mass = s[0];
+  if (momentum) {
+    momentum[0] = s[1];
+    momentum[1] = s[2];
+    momentum[2] = s[3];
+  }
+  return CFLBM_OK;
+}
+
+int cflbm_get_f(cflbm_handle *h, double *out) {
+  if (!h || !out) return fail(CFLBM_E_INVALID, "bad arguments");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t n = (size_t)h->Q * h->L.nx * h->L.ny * h->L.nz;
+  double *d = nullptr;
+  CK_CUDA(cudaMalloc(&d, n * sizeof(double)));
+  cudaError_t e = launch_get_f(h->Q, h->cfg.storage, h->L, h->fA, d, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CK_CUDA(e);
+  return CFLBM_OK;
+}
+
+int cflbm_set_f(cflbm_handle *h, const double *in, int64_t steps_done) {
+  if (!h || !in || steps_done < 0) return fail(CFLBM_E_INVALID, "bad arguments");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t n = (size_t)h->Q * h->L.nx * h->L.ny * h->L.nz;
+  double *d = nullptr;
+  CK_CUDA(cudaMalloc(&d, n * sizeof(double)));
+  cudaError_t e = cudaMemcpyAsync(d, in, n * 8, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = launch_set_f(h->Q, h->cfg.storage, h->L, h->fA, d, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CK_CUDA(e);
+  h->steps_done = steps_done;
+  long long st = steps_done;
+  CK_CUDA(cudaMemcpy(h->d_step, &st, sizeof(st), cudaMemcpyHostToDevice));
+  return CFLBM_OK;
+}
+
+int cflbm_get_info(cflbm_handle *h, cflbm_info *info) {
+  if (!h || !info) return fail(CFLBM_E_INVALID, "bad arguments");
+  std::memset(info, 0, sizeof(*info));
+  info->lattice = h->Q;
+  info->nx = h->L.nx;
+  info->ny = h->L.ny;
+  info->nz = h->L.nz;
+  info->storage = h->cfg.storage;
+  info->compute = h->cfg.compute;
+  info->profile = h->cfg.profile;
+  info->ghost = h->L.G;
+  info->pitch_x = h->L.px;
+  info->pop_stride = h->L.S;
+  info->steps_done = h->steps_done;
+  info->n_links = h->n_links;
+  info->n_solid = h->n_solid;
+  info->omega = h->omega;
+  info->bytes_per_cell_step = 2.0 * h->Q * h->esize + 0.125;
+  info->device_bytes = h->device_bytes;
+  return CFLBM_OK;
+}
+
+int cflbm_write_tecplot(cflbm_handle *h, const char *path, int n) {
+  if (!h || !path) return fail(CFLBM_E_INVALID, "bad arguments");
+  const size_t N = (size_t)h->L.nx * h->L.ny * h->L.nz;
+  std::vector<double> u(N), v(N), w(N), p(N);
+  int rc = cflbm_macros(h, u.data(), v.data(), w.data(), p.data());
+  if (rc) return rc;
+  rc = write_tecplot(path, h->Q == 27 ? 3 : 2, h->L.nx, h->L.ny, h->L.nz, u.data(), v.data(),
+                     w.data(), p.data(), n);
+  if (rc) return fail(rc, "writing %s failed", path);
+  return CFLBM_OK;
+}
+
+int cflbm_get_stream(cflbm_handle *h, void **stream) {
+  if (!h || !stream) return fail(CFLBM_E_INVALID, "bad arguments");
+  *stream = (void *)h->stream;
+  return CFLBM_OK;
+}
+
+int cflbm_set_timing(cflbm_handle *h, int enable) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  h->timing = enable != 0;
+  return CFLBM_OK;
+}
+
+int cflbm_get_timing(cflbm_handle *h, double ms[2], int64_t counts[2]) {
+  if (!h || !ms || !counts) return fail(CFLBM_E_INVALID, "bad arguments");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  double tot[2] = {0.0, 0.0};
+  const std::vector<std::pair<size_t, size_t>> *lists[2] = {&h->sweep_ev, &h->bnd_ev};
+  for (int k = 0; k < 2; ++k)
+    for (const auto &pr : *lists[k]) {
+      float t = 0.f;
+      CK_CUDA(cudaEventElapsedTime(&t, h->ev_pool[pr.first], h->ev_pool[pr.second]));
+      tot[k] += t;
+    }
+  ms[0] = tot[0];
+  ms[1] = tot[1];
+  counts[0] = (int64_t)h->sweep_ev.size();
+  counts[1] = (int64_t)h->bnd_ev.size();
+  h->sweep_ev.clear();
+  h->bnd_ev.clear();
+  h->ev_used = 0;
+  return CFLBM_OK;
+}
+
+int cflbm_write_tecplot_fields(const char *path, int dim, int nx, int ny, int nz,
+                               const double *u, const double *v, const double *w,
+                               const double *p, int n) {
+  if (!path || !u || !v || !p || (dim == 3 && !w) || (dim != 2 && dim != 3) || nx < 2 ||
+      ny < 2 || (dim == 3 && nz < 2))
+    return fail(CFLBM_E_INVALID, "bad arguments");
+  int rc = write_tecplot(path, dim, nx, ny, dim == 3 ? nz : 1, u, v, w, p, n);
+  if (rc) return fail(rc, "writing %s failed", path);
+  return CFLBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,546 @@
+// Boundary, bounce-back/force, initialisation and reduction kernels.
+//
+// These run on O(surface) work (ghost layers, fluid->solid links) except the
+// initialisation, reduction and dump/restore kernels, which run once or on
+// demand.  The hot per-step sweep is in sweep.cuh.
+#include <cstdio>
+#include "solver.cuh"
+
+namespace cflbm {
+
+namespace {
+
+long long g_launches = 0;
+
+// Runtime direction tables (boundary kernels index directions dynamically).
+template <int Q> struct DT;
+template <> struct DT<9> {
+  __device__ static int ex(int i) {
+    const int v[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    return v[i];
+  }
+  __device__ static int ey(int i) {
+    const int v[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    return v[i];
+  }
+  __device__ static int ez(int) { return 0; }
+};
+__constant__ signed char c_e27[27][3] = {
+    {0, 0, 0},  {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},   {0, -1, 0},  {0, 0, 1},   {0, 0, -1},
+    {1, 1, 0},  {-1, -1, 0}, {1, -1, 0}, {-1, 1, 0},  {1, 0, 1},   {-1, 0, -1}, {1, 0, -1},
+    {-1, 0, 1}, {0, 1, 1},   {0, -1, -1}, {0, 1, -1}, {0, -1, 1},  {1, 1, 1},   {-1, -1, -1},
+    {1, -1, 1}, {-1, 1, -1}, {1, 1, -1}, {-1, -1, 1}, {1, -1, -1}, {-1, 1, 1}};
+template <> struct DT<27> {
+  __device__ static int ex(int i) { return c_e27[i][0]; }
+  __device__ static int ey(int i) { return c_e27[i][1]; }
+  __device__ static int ez(int i) { return c_e27[i][2]; }
+};
+template <int Q> __device__ int dopp(int i) { return Lat<Q>::opp(i); }
+template <int Q> __device__ int dmirror(int i, int d) {
+  int w0 = DT<Q>::ex(i), w1 = DT<Q>::ey(i), w2 = DT<Q>::ez(i);
+  if (d == 1) w1 = -w1;
+  if (d == 2) w2 = -w2;
+  if (d == 0) w0 = -w0;
+  for (int k = 0; k < Q; ++k)
+    if (DT<Q>::ex(k) == w0 && DT<Q>::ey(k) == w1 && DT<Q>::ez(k) == w2) return k;
+  return i;
+}
+
+template <class ST> struct Dec;
+template <> struct Dec<double> {
+  template <int Q> __device__ static double get(double v, int) { return v; }
+  template <int Q> __device__ static double put(double v, int) { return v; }
+};
+template <> struct Dec<float> {
+  template <int Q> __device__ static double get(float v, int) { return (double)v; }
+  template <int Q> __device__ static float put(double v, int) { return (float)v; }
+};
+template <> struct Dec<F16Dev> {
+  template <int Q> __device__ static double get(__half v, int i) {
+    return (double)__half2float(v) / (double)Lat<Q>::h_scale(i);
+  }
+  template <int Q> __device__ static __half put(double v, int i) {
+    return __float2half_rn((float)(v * (double)Lat<Q>::h_scale(i)));
+  }
+};
+
+inline int blocks_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 65535LL * 8) b = 65535LL * 8;
+  return (int)b;
+}
+
+// ---- channel-profile ghost fill ------------------------------------------------
+// Post-stream value of direction i0 at interior cell X (pull from S = X - e_i0):
+//   z out of range: periodic wrap, or free-slip mirror (i := mirror_z(i),
+//   S.z := X.z), or no-slip (halfway bounce-back: f*_{opp(i0)}(X));
+//   then the same for y; then S.x < 0 -> inlet equilibrium, S.x >= nx -> x := nx-1
+//   (zero gradient); a solid source -> f*_{opp(i0)}(X).
+template <int Q, class E>
+__device__ E resolve_channel(const E *f, const FillArgs &a, int i0, int x, int y, int z) {
+  const Layout &L = a.L;
+  int i = i0;
+  int sx = x - DT<Q>::ex(i0), sy = y - DT<Q>::ey(i0), sz = z - DT<Q>::ez(i0);
+  if (Q == 27 && (sz < 0 || sz >= L.nz)) {
+    if (a.wall_z == WALL_PERIODIC) sz = (sz + L.nz) % L.nz;
+    else if (a.wall_z == WALL_FREESLIP) { i = dmirror<Q>(i, 2); sz = z; }
+    else return f[dopp<Q>(i0) * L.S + L.idx(x, y, z)];
+  }
+  if (sy < 0 || sy >= L.ny) {
+    if (a.wall_y == WALL_PERIODIC) sy = (sy + L.ny) % L.ny;
+    else if (a.wall_y == WALL_FREESLIP) { i = dmirror<Q>(i, 1); sy = y; }
+    else return f[dopp<Q>(i0) * L.S + L.idx(x, y, z)];
+  }
+  if (sx < 0) return static_cast<const E *>(a.f_in)[i];
+  if (sx >= L.nx) sx = L.nx - 1;
+  if (mask_solid(a.mask, a.nxw, L.ny, sx, sy, sz)) return f[dopp<Q>(i0) * L.S + L.idx(x, y, z)];
+  return f[i * L.S + L.idx(sx, sy, sz)];
+}
+
+template <int Q, class ST>
+__global__ void fill_channel_kernel(const FillArgs a) {
+  using E = typename Store<ST>::elem;
+  E *f = static_cast<E *>(a.f);
+  const Layout &L = a.L;
+  const bool d3 = (Q == 27);
+  const long long zr = d3 ? (L.nz + 2) : 1;
+  const long long nfx = (long long)(L.ny + 2) * zr;
+  const long long nfy = (long long)L.nx * zr;
+  const long long nfz = d3 ? (long long)L.nx * L.ny : 0;
+  const long long total = 2 * (nfx + nfy + nfz);
+  const int z0 = d3 ? -1 : 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long r = t;
+    int sx, sy, sz;
+    if (r < 2 * nfx) {
+      const int side = (int)(r / nfx);
+      r %= nfx;
+      sx = side ? L.nx : -1;
+      sy = (int)(r % (L.ny + 2)) - 1;
+      sz = (int)(r / (L.ny + 2)) + z0;
+    } else if ((r -= 2 * nfx) < 2 * nfy) {
+      const int side = (int)(r / nfy);
+      r %= nfy;
+      sy = side ? L.ny : -1;
+      sx = (int)(r % L.nx);
+      sz = (int)(r / L.nx) + z0;
+    } else {
+      r -= 2 * nfy;
+      const long long nfzd = nfz > 0 ? nfz : 1;
+      const int side = (int)(r / nfzd);
+      r %= nfzd;
+      sz = side ? L.nz : -1;
+      sx = (int)(r % L.nx);
+      sy = (int)(r / L.nx);
+    }
+    const long long sidx = L.idx(sx, sy, sz);
+    for (int i = 1; i < Q; ++i) {
+      const int X = sx + DT<Q>::ex(i), Y = sy + DT<Q>::ey(i), Z = sz + DT<Q>::ez(i);
+      if (!L.interior(X, Y, Z)) continue;
+      f[i * L.S + sidx] = resolve_channel<Q, E>(f, a, i, X, Y, Z);
+    }
+  }
+}
+
+// ---- reference-profile face passes -------------------------------------------
+// One pass of the reference's Streaming() boundary sequence over a face:
+//   copy   (x low,  e_x > 0): f_i(-1, j, k)  = f_i(0, j, k)
+//          ("3D MPI+KOKKOS+MPIIO/lbm.cpp:326-335", "MPI Kokkos/lbm.cpp:315-321")
+//   extrap (x high, e_x < 0): f_i(nx, j, k) = f_i(nx-1, j+e_y, k+e_z)    (:338-347, :323-329)
+//   bounce (wall, e_a pointing inward): the ghost layer takes the opposite
+//          population two layers in, shifted by twice the in-plane velocity
+//          (:278-324, :331-345).
+// Tangential ranges cover the interior plus one ring, [-1, n+1), as the
+// reference's [ghost-1, l-ghost+1).
+template <int Q, class ST>
+__global__ void face_op_kernel(const FillArgs a, const FaceOp op) {
+  using E = typename Store<ST>::elem;
+  E *f = static_cast<E *>(a.f);
+  const Layout &L = a.L;
+  const bool d3 = (Q == 27);
+  const int n[3] = {L.nx, L.ny, L.nz};
+  const int ta = (op.axis == 0) ? 1 : 0;
+  const int tb = (op.axis == 2) ? 1 : 2;
+  const int na = n[ta] + 2;
+  const int nb = d3 ? n[tb] + 2 : 1;
+  const int b0 = d3 ? -1 : 0;
+  const long long total = (long long)na * nb;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int pa = (int)(t % na) - 1;
+    const int pb = (int)(t / na) + b0;
+    for (int i = 0; i < Q; ++i) {
+      const int e[3] = {DT<Q>::ex(i), DT<Q>::ey(i), DT<Q>::ez(i)};
+      const int ea = e[op.axis];
+      int dst[3], src[3];
+      int srcpop = i;
+      dst[ta] = pa;
+      dst[tb] = pb;
+      if (op.kind == 0) {
+        if (ea <= 0) continue;
+        dst[op.axis] = -1;
+        src[0] = 0; src[ta] = pa; src[tb] = pb;
+      } else if (op.kind == 1) {
+        if (ea >= 0) continue;
+        dst[op.axis] = n[op.axis];
+        src[0] = n[0] - 1;
+        src[ta] = pa + e[ta];
+        src[tb] = pb + e[tb];
+      } else {
+        if (op.side == 0 ? (ea <= 0) : (ea >= 0)) continue;
+        dst[op.axis] = op.side == 0 ? -1 : n[op.axis];
+        src[op.axis] = op.side == 0 ? 1 : n[op.axis] - 2;
+        src[ta] = pa + 2 * e[ta];
+        src[tb] = pb + 2 * e[tb];
+        srcpop = dopp<Q>(i);
+      }
+      if (!d3) { dst[2] = 0; src[2] = 0; }
+      f[i * L.S + L.idx(dst[0], dst[1], dst[2])] =
+          f[srcpop * L.S + L.idx(src[0], src[1], src[2])];
+    }
+  }
+}
+
+// Keep the ghost layers of the single-array reference semantics: after the sweep
+// wrote B's interior, B's ghosts take A's (so values a pass does not rewrite
+// persist from step to step, as in the reference's one f array).
+template <int Q, class ST>
+__global__ void ghost_copy_kernel(const Layout L, const void *src_, void *dst_) {
+  using E = typename Store<ST>::elem;
+  const E *src = static_cast<const E *>(src_);
+  E *dst = static_cast<E *>(dst_);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.S;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(e % L.px) - L.xoff;
+    const long long r = e / L.px;
+    const int y = (int)(r % L.nyp) - L.G;
+    const int z = (int)(r / L.nyp) - L.Gz;
+    if (L.interior(x, y, z)) continue;
+#pragma unroll 9
+    for (int i = 0; i < Q; ++i) dst[i * L.S + e] = src[i * L.S + e];
+  }
+}
+
+// ---- solid links: bounce-back fill + momentum-exchange force ----------------
+// For link (s, k): s solid, X = s + e_k fluid.  Fill f_k(s) = f*_{opp(k)}(s +
+// reach*e_k) (reach 1: halfway bounce-back; reach 2: the reference's usrbc,
+// "3D.../lbm.cpp:350-356", "MPI Kokkos/lbm.cpp:347-353").  Force: the reference's
+// momentum exchange ("MPI Kokkos/lbm.cpp:364-377") sums, over fluid X and
+// direction ii = opp(k) pointing into the solid, (f_ii(X) + f_opp(ii)(X + e_ii))
+// e_ii after the fill.  Reduced per block in FP64, then by the last block in
+// block order (deterministic), into the force history slot of this step.
+template <int Q, class ST>
+__global__ void links_kernel(const LinkArgs a) {
+  using E = typename Store<ST>::elem;
+  E *f = static_cast<E *>(a.f);
+  const Layout &L = a.L;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < a.n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int4 l = a.links[t];
+    const int k = l.w, kb = dopp<Q>(k);
+    const long long ok = L.off(DT<Q>::ex(k), DT<Q>::ey(k), DT<Q>::ez(k));
+    const long long s = L.idx(l.x, l.y, l.z);
+    const E v = f[kb * L.S + s + a.reach * ok];
+    f[k * L.S + s] = v;
+    const double m = Dec<ST>::template get<Q>(f[kb * L.S + s + ok], kb) +
+                     Dec<ST>::template get<Q>(v, kb);
+    fx += m * DT<Q>::ex(kb);
+    fy += m * DT<Q>::ey(kb);
+    fz += m * DT<Q>::ez(kb);
+  }
+  __shared__ double sh[3][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    fx += __shfl_down_sync(0xffffffffu, fx, o);
+    fy += __shfl_down_sync(0xffffffffu, fy, o);
+    fz += __shfl_down_sync(0xffffffffu, fz, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][wid] = fx; sh[1][wid] = fy; sh[2][wid] = fz; }
+  __syncthreads();
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    double bx = 0, by = 0, bz = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { bx += sh[0][w]; by += sh[1][w]; bz += sh[2][w]; }
+    a.partials[3 * blockIdx.x] = bx;
+    a.partials[3 * blockIdx.x + 1] = by;
+    a.partials[3 * blockIdx.x + 2] = bz;
+    __threadfence();
+    last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double bx = 0, by = 0, bz = 0;
+    const volatile double *p = a.partials;
+    for (unsigned b = 0; b < gridDim.x; ++b) { bx += p[3 * b]; by += p[3 * b + 1]; bz += p[3 * b + 2]; }
+    const long long st = *a.step;
+    double *h = a.hist + 3 * (st % a.cap);
+    h[0] = bx;
+    h[1] = by;
+    h[2] = bz;
+    *a.step = st + 1;
+    *a.counter = 0u;
+  }
+}
+
+// ---- initialisation ---------------------------------------------------------------
+// f = feq(p, u) over the whole ghosted box from host-computed macroscopic fields
+// (reference profiles: "3D.../lbm.cpp:245-254", "MPI Kokkos/lbm.cpp:116-124").
+template <int Q, class ST>
+__global__ void init_macros_kernel(const Layout L, void *f_, const double *u, const double *v,
+                                   const double *w, const double *p) {
+  using E = typename Store<ST>::elem;
+  E *f = static_cast<E *>(f_);
+  const int lxp = L.nx + 2 * L.G, lyp = L.ny + 2 * L.G, lzp = L.nz + 2 * L.Gz;
+  const long long total = (long long)lxp * lyp * lzp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % lxp) - L.G;
+    const int y = (int)((t / lxp) % lyp) - L.G;
+    const int z = (int)(t / ((long long)lxp * lyp)) - L.Gz;
+    const double uu = u[t], vv = v[t], ww = w[t], pp = p[t];
+    const long long c = L.idx(x, y, z);
+    for (int i = 0; i < Q; ++i) {
+      const double edu = DT<Q>::ex(i) * uu + DT<Q>::ey(i) * vv + DT<Q>::ez(i) * ww;
+      const double udu = uu * uu + vv * vv + ww * ww;
+      const double feq =
+          Lat<Q>::w(i) * pp * 3.0 + Lat<Q>::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * udu);
+      f[i * L.S + c] = Dec<ST>::template put<Q>(feq, i);
+    }
+  }
+}
+
+// Channel profile: p = 0, u = (u_in, seeded perturbation, 0) in fluid, 0 in
+// solids; f = feq.  Also records these as the step-0 macroscopic fields.
+template <int Q, class ST>
+__global__ void init_channel_kernel(const Layout L, void *f_, const uint32_t *mask, int nxw,
+                                    double u_in, double amp, unsigned long long seed,
+                                    double *mu, double *mv, double *mw, double *mp) {
+  using E = typename Store<ST>::elem;
+  E *f = static_cast<E *>(f_);
+  const long long total = (long long)L.nx * L.ny * L.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % L.nx);
+    const int y = (int)((t / L.nx) % L.ny);
+    const int z = (int)(t / ((long long)L.nx * L.ny));
+    const bool solid = mask_solid(mask, nxw, L.ny, x, y, z);
+    const double uu = solid ? 0.0 : u_in;
+    const double vv = solid ? 0.0 : perturbation(seed, t, amp);
+    mu[t] = uu;
+    mv[t] = vv;
+    mw[t] = 0.0;
+    mp[t] = 0.0;
+    const long long c = L.idx(x, y, z);
+    for (int i = 0; i < Q; ++i) {
+      const double edu = DT<Q>::ex(i) * uu + DT<Q>::ey(i) * vv;
+      const double udu = uu * uu + vv * vv;
+      const double feq = Lat<Q>::w(i) * 0.0 * 3.0 +
+                         Lat<Q>::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * udu);
+      f[i * L.S + c] = Dec<ST>::template put<Q>(feq, i);
+    }
+  }
+}
+
+// ---- FP64 domain sums (mass = sum of rho over fluid, momentum) ------------------
+template <int Q, class ST>
+__global__ void reduce_mass_kernel(const ReduceArgs a) {
+  using E = typename Store<ST>::elem;
+  const E *f = static_cast<const E *>(a.f);
+  const Layout &L = a.L;
+  const long long total = (long long)L.nx * L.ny * L.nz;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % L.nx);
+    const int y = (int)((t / L.nx) % L.ny);
+    const int z = (int)(t / ((long long)L.nx * L.ny));
+    if (mask_solid(a.mask, a.nxw, L.ny, x, y, z)) continue;
+    const long long c = L.idx(x, y, z);
+    double r = 1.0;
+    for (int i = 0; i < Q; ++i) {
+      const double fi = Dec<ST>::template get<Q>(f[i * L.S + c], i);
+      r += fi;
+      acc[1] += fi * DT<Q>::ex(i);
+      acc[2] += fi * DT<Q>::ey(i);
+      acc[3] += fi * DT<Q>::ez(i);
+    }
+    acc[0] += r;
+  }
+  __shared__ double sh[4][32];
+  for (int o = 16; o > 0; o >>= 1)
+    for (int q = 0; q < 4; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int q = 0; q < 4; ++q) sh[q][wid] = acc[q];
+  __syncthreads();
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 4; ++q) {
+      double b = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += sh[q][w];
+      a.partials[4 * blockIdx.x + q] = b;
+    }
+    __threadfence();
+    last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const volatile double *p = a.partials;
+    for (int q = 0; q < 4; ++q) {
+      double s = 0.0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += p[4 * b + q];
+      a.out[q] = s;
+    }
+    *a.counter = 0u;
+  }
+}
+
+// ---- dump / restore --------------------------------------------------------------
+template <int Q, class ST>
+__global__ void get_f_kernel(const Layout L, const void *f_, double *out) {
+  using E = typename Store<ST>::elem;
+  const E *f = static_cast<const E *>(f_);
+  const long long N = (long long)L.nx * L.ny * L.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N * Q;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N);
+    const long long n = t % N;
+    const int x = (int)(n % L.nx);
+    const int y = (int)((n / L.nx) % L.ny);
+    const int z = (int)(n / ((long long)L.nx * L.ny));
+    out[t] = Dec<ST>::template get<Q>(f[i * L.S + L.idx(x, y, z)], i);
+  }
+}
+
+template <int Q, class ST>
+__global__ void set_f_kernel(const Layout L, void *f_, const double *in) {
+  using E = typename Store<ST>::elem;
+  E *f = static_cast<E *>(f_);
+  const long long N = (long long)L.nx * L.ny * L.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N * Q;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N);
+    const long long n = t % N;
+    const int x = (int)(n % L.nx);
+    const int y = (int)((n / L.nx) % L.ny);
+    const int z = (int)(n / ((long long)L.nx * L.ny));
+    f[i * L.S + L.idx(x, y, z)] = Dec<ST>::template put<Q>(in[t], i);
+  }
+}
+
+}  // namespace
+
+long long launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+void count_launch(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
+
+cudaError_t launch_sweep_q9(int store, int compute, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_sweep_q27(int store, int compute, const SweepArgs &a, cudaStream_t s);
+
+cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cudaStream_t s) {
+  return Q == 9 ? launch_sweep_q9(store, compute, a, s) : launch_sweep_q27(store, compute, a, s);
+}
+
+// Dispatch helper: run F<Q, ST> for the runtime (Q, store).
+#define CFLBM_DISPATCH(Q, store, CALL)                                   \
+  do {                                                                   \
+    if ((Q) == 9) {                                                      \
+      constexpr int QQ = 9;                                              \
+      if ((store) == STORE_F64) { using ST = double; CALL; }             \
+      else if ((store) == STORE_F32) { using ST = float; CALL; }         \
+      else { using ST = F16Dev; CALL; }                                  \
+    } else {                                                             \
+      constexpr int QQ = 27;                                             \
+      if ((store) == STORE_F64) { using ST = double; CALL; }             \
+      else if ((store) == STORE_F32) { using ST = float; CALL; }         \
+      else { using ST = F16Dev; CALL; }                                  \
+    }                                                                    \
+  } while (0)
+
+cudaError_t launch_fill_channel(int Q, int store, const FillArgs &a, cudaStream_t s) {
+  const bool d3 = Q == 27;
+  const long long zr = d3 ? a.L.nz + 2 : 1;
+  const long long total = 2 * ((a.L.ny + 2) * zr + (long long)a.L.nx * zr +
+                               (d3 ? (long long)a.L.nx * a.L.ny : 0));
+  const int blocks = blocks_for(total, 128);
+  CFLBM_DISPATCH(Q, store, (fill_channel_kernel<QQ, ST><<<blocks, 128, 0, s>>>(a)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaStream_t s) {
+  const int n[3] = {a.L.nx, a.L.ny, a.L.nz};
+  const int ta = (op.axis == 0) ? 1 : 0, tb = (op.axis == 2) ? 1 : 2;
+  const long long total = (long long)(n[ta] + 2) * (Q == 27 ? n[tb] + 2 : 1);
+  const int blocks = blocks_for(total, 128);
+  CFLBM_DISPATCH(Q, store, (face_op_kernel<QQ, ST><<<blocks, 128, 0, s>>>(a, op)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_copy(int Q, int store, const Layout &L, const void *src, void *dst,
+                              cudaStream_t s) {
+  const int blocks = blocks_for(L.S, 256);
+  CFLBM_DISPATCH(Q, store, (ghost_copy_kernel<QQ, ST><<<blocks, 256, 0, s>>>(L, src, dst)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_links(int Q, int store, const LinkArgs &a, int blocks, cudaStream_t s) {
+  CFLBM_DISPATCH(Q, store, (links_kernel<QQ, ST><<<blocks, 256, 0, s>>>(a)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_macros(int Q, int store, const Layout &L, void *f, const double *u,
+                               const double *v, const double *w, const double *p,
+                               cudaStream_t s) {
+  const long long total =
+      (long long)(L.nx + 2 * L.G) * (L.ny + 2 * L.G) * (L.nz + 2 * L.Gz);
+  const int blocks = blocks_for(total, 256);
+  CFLBM_DISPATCH(Q, store,
+                 (init_macros_kernel<QQ, ST><<<blocks, 256, 0, s>>>(L, f, u, v, w, p)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_channel(int Q, int store, const Layout &L, void *f,
+                                const uint32_t *mask, int nxw, double u_in, double amp,
+                                unsigned long long seed, double *mu, double *mv, double *mw,
+                                double *mp, cudaStream_t s) {
+  const int blocks = blocks_for((long long)L.nx * L.ny * L.nz, 256);
+  CFLBM_DISPATCH(Q, store,
+                 (init_channel_kernel<QQ, ST><<<blocks, 256, 0, s>>>(
+                     L, f, mask, nxw, u_in, amp, seed, mu, mv, mw, mp)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_mass(int Q, int store, const ReduceArgs &a, int blocks,
+                               cudaStream_t s) {
+  CFLBM_DISPATCH(Q, store, (reduce_mass_kernel<QQ, ST><<<blocks, 256, 0, s>>>(a)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_get_f(int Q, int store, const Layout &L, const void *f, double *out,
+                         cudaStream_t s) {
+  const int blocks = blocks_for((long long)L.nx * L.ny * L.nz * Q, 256);
+  CFLBM_DISPATCH(Q, store, (get_f_kernel<QQ, ST><<<blocks, 256, 0, s>>>(L, f, out)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_f(int Q, int store, const Layout &L, void *f, const double *in,
+                         cudaStream_t s) {
+  const int blocks = blocks_for((long long)L.nx * L.ny * L.nz * Q, 256);
+  CFLBM_DISPATCH(Q, store, (set_f_kernel<QQ, ST><<<blocks, 256, 0, s>>>(L, f, in)));
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace cflbm

@@ -1,0 +1,67 @@
+// Internal handle state and host-side helpers shared by the C ABI sources.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "../../include/cflbm.h"
+#include "solver.cuh"
+
+struct cflbm_handle {
+  cflbm_config cfg{};
+  int Q = 9;
+  cflbm::Layout L{};
+  int nxw = 0;
+  int esize = 8;
+  cudaStream_t stream = nullptr;
+  void *fA = nullptr, *fB = nullptr;
+  size_t f_bytes = 0;
+  uint32_t *d_mask = nullptr;
+  int4 *d_links = nullptr;
+  long long n_links = 0;
+  long long n_solid = 0;
+  double *d_mu = nullptr, *d_mv = nullptr, *d_mw = nullptr, *d_mp = nullptr;
+  double *d_inlet = nullptr;
+  float *d_alpha = nullptr;
+  void *d_fin = nullptr;
+  double *d_hist = nullptr;
+  long long hist_cap = 0;
+  long long *d_step = nullptr;
+  double *d_partials = nullptr;
+  int link_blocks = 1;
+  int reduce_blocks = 1;
+  unsigned int *d_counter = nullptr;   // links kernel
+  unsigned int *d_counter2 = nullptr;  // mass kernel
+  double *d_sums = nullptr;            // 4 doubles (mass, momentum)
+  long long steps_done = 0;
+  double omega = 1.0;
+  double area = 1.0;  // Cd/Cl reference area
+  size_t device_bytes = 0;
+  // Kernel timing (cflbm_set_timing): event pairs around sweeps / boundary phases.
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<size_t, size_t>> sweep_ev, bnd_ev;
+};
+
+namespace cflbm {
+
+// Host-side set-up of the reference profiles (reference_setup.cpp).
+struct RefSetup {
+  std::vector<uint8_t> solid;  // interior mask, x fastest
+  std::vector<double> u, v, w, p;  // ghosted box, x fastest
+  std::vector<double> inlet;   // ny*nz inlet override profile
+  double area = 1.0;
+};
+int ref2d_setup(int nx, int ny, double u0, const int32_t *ran, RefSetup &out);
+int ref3d_setup(int nx, int ny, int nz, double u0, const int32_t *ran, RefSetup &out);
+
+// Channel mask from the configured geometry (reference_setup.cpp).
+void channel_mask(const cflbm_config &c, std::vector<uint8_t> &solid);
+double channel_area(const cflbm_config &c);
+
+// Tecplot binary writer (tecplot.cpp).
+int write_tecplot(const char *path, int dim, int nx, int ny, int nz, const double *u,
+                  const double *v, const double *w, const double *p, int n);
+
+}  // namespace cflbm

@@ -1,0 +1,129 @@
+// Lattice tables and population storage formats, usable from host and device.
+//
+// Velocity order, weights and bounce-back pairs follow the reference exactly so
+// that population index i means the same direction everywhere:
+//   D2Q9  "Kokkos/lbm.cpp:57-95": 0, E, N, W, S, NE, NW, SW, SE;
+//   D3Q27 "3D MPI+KOKKOS+MPIIO/lbm.cpp:55-218": rest, then +/- pairs (2k-1, 2k).
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+
+namespace cflbm {
+
+template <int Q> struct Lat;
+
+template <> struct Lat<9> {
+  static constexpr int Q = 9;
+  static constexpr int D = 2;
+  __host__ __device__ static constexpr int ex(int i) {
+    constexpr int v[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ey(int i) {
+    constexpr int v[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ez(int) { return 0; }
+  __host__ __device__ static constexpr int opp(int i) {
+    constexpr int v[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double w(int i) {
+    return i == 0 ? 4.0 / 9.0 : (i < 5 ? 1.0 / 9.0 : 1.0 / 36.0);
+  }
+  // The (i, opp(i)) pairs with i < opp(i).
+  static constexpr int NPAIR = 4;
+  __host__ __device__ static constexpr int pair(int k) {
+    constexpr int v[4] = {1, 2, 5, 6};
+    return v[k];
+  }
+  // Power-of-two scale close to 1/w_i used by the FP16 deviation format.
+  __host__ __device__ static constexpr float h_scale(int i) {
+    return i == 0 ? 2.0f : (i < 5 ? 8.0f : 32.0f);
+  }
+};
+
+template <> struct Lat<27> {
+  static constexpr int Q = 27;
+  static constexpr int D = 3;
+  __host__ __device__ static constexpr int ex(int i) {
+    constexpr int v[27] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1,
+                           -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ey(int i) {
+    constexpr int v[27] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0,
+                           0, 1, -1, 1, -1, 1, -1, -1, 1, 1, -1, -1, 1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ez(int i) {
+    constexpr int v[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1,
+                           1, 1, -1, -1, 1, 1, -1, 1, -1, -1, 1, -1, 1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int opp(int i) {
+    return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1);
+  }
+  __host__ __device__ static constexpr double w(int i) {
+    return i == 0 ? 8.0 / 27.0 : (i <= 6 ? 2.0 / 27.0 : (i <= 18 ? 1.0 / 54.0 : 1.0 / 216.0));
+  }
+  static constexpr int NPAIR = 13;
+  __host__ __device__ static constexpr int pair(int k) { return 2 * k + 1; }
+  __host__ __device__ static constexpr float h_scale(int i) {
+    return i == 0 ? 4.0f : (i <= 6 ? 16.0f : (i <= 18 ? 64.0f : 256.0f));
+  }
+};
+
+// Direction with the component along axis d reversed (specular reflection).
+template <class L>
+__host__ __device__ constexpr int mirror(int i, int d) {
+  int w0 = L::ex(i), w1 = L::ey(i), w2 = L::ez(i);
+  if (d == 0) w0 = -w0;
+  if (d == 1) w1 = -w1;
+  if (d == 2) w2 = -w2;
+  for (int k = 0; k < L::Q; ++k)
+    if (L::ex(k) == w0 && L::ey(k) == w1 && L::ez(k) == w2) return k;
+  return -1;
+}
+
+// ---- storage formats ---------------------------------------------------------
+// Store<T>::load/store convert between the stored element and the arithmetic
+// type A; FP16 deviation storage keeps f_i * h_scale(i) in binary16.
+struct F16Dev {
+  __half h;
+};
+
+template <class T> struct Store;
+
+#if defined(__CUDACC__)
+
+template <> struct Store<double> {
+  using elem = double;
+  template <class A, class L>
+  __device__ static A load(const elem *p, int) { return static_cast<A>(__ldg(p)); }
+  template <class A, class L>
+  __device__ static void store(elem *p, A v, int) { *p = static_cast<double>(v); }
+};
+
+template <> struct Store<float> {
+  using elem = float;
+  template <class A, class L>
+  __device__ static A load(const elem *p, int) { return static_cast<A>(__ldg(p)); }
+  template <class A, class L>
+  __device__ static void store(elem *p, A v, int) { *p = static_cast<float>(v); }
+};
+
+template <> struct Store<F16Dev> {
+  using elem = __half;
+  template <class A, class L>
+  __device__ static A load(const elem *p, int i) {
+    return static_cast<A>(__half2float(__ldg(p)) * (1.0f / L::h_scale(i)));
+  }
+  template <class A, class L>
+  __device__ static void store(elem *p, A v, int i) {
+    *p = __float2half_rn(static_cast<float>(v) * L::h_scale(i));
+  }
+};
+#endif  // __CUDACC__
+
+}  // namespace cflbm

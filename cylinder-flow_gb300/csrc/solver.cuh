@@ -1,0 +1,138 @@
+// Internal device-side declarations of the cylinder-flow solver.
+//
+// Data layout in HBM (one array per population buffer, two buffers A/B):
+//   f[i][z + Gz][y + G][x + xoff]  (structure of arrays, x fastest)
+// with i the population, G ghost layers around the interior in x and y (and z in
+// 3-D), rows padded to `px` elements so every interior row starts on a 128-byte
+// boundary.  A holds the post-collision populations of the current step; the
+// sweep pulls from A and writes the next post-collision state into B; the
+// buffers then swap.  The ghost layers and the populations of solid cells that
+// face fluid are refilled before each sweep by the boundary kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "lattice.cuh"
+
+namespace cflbm {
+
+enum Profile { PROFILE_CHANNEL = 0, PROFILE_REF2D = 1, PROFILE_REF3D = 2 };
+enum Wall { WALL_FREESLIP = 0, WALL_NOSLIP = 1, WALL_PERIODIC = 2 };
+enum StoreKind { STORE_F64 = 0, STORE_F32 = 1, STORE_F16 = 2 };
+enum ComputeKind { COMPUTE_F64 = 0, COMPUTE_F32 = 1 };
+
+struct Layout {
+  int nx, ny, nz;  // interior cells (nz = 1 in 2-D)
+  int G, Gz;       // ghost layers in x/y and in z (0 in 2-D)
+  int xoff;        // element offset of interior x = 0 inside a row
+  int px;          // row pitch in elements
+  int nyp, nzp;    // padded y and z extents
+  long long S;     // elements per population
+  __host__ __device__ long long idx(int x, int y, int z) const {
+    return ((long long)(z + Gz) * nyp + (y + G)) * px + (x + xoff);
+  }
+  __host__ __device__ long long off(int ex, int ey, int ez) const {
+    return (long long)ex + (long long)px * ((long long)ey + (long long)nyp * ez);
+  }
+  __host__ __device__ bool interior(int x, int y, int z) const {
+    return x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz;
+  }
+};
+
+__host__ __device__ inline bool mask_solid(const uint32_t *m, int nxw, int ny, int x, int y, int z) {
+  return (m[((long long)z * ny + y) * nxw + (x >> 5)] >> (x & 31)) & 1u;
+}
+
+struct SweepArgs {
+  Layout L;
+  const void *fa;        // post-collision state of this step (ghosts filled)
+  void *fb;              // next post-collision state
+  const uint32_t *mask;  // bit-packed interior solid mask
+  int nxw;               // mask words per row
+  float omega_f;
+  double omega;
+  int ref_override;      // reference profiles: inlet u at x = 0, p = 0 at x = nx-1
+  const double *inlet_u; // ny*nz inlet velocity profile (reference profiles)
+  const float *alpha;    // nx*ny*nz Brinkman porosity or null
+  double *mu, *mv, *mw, *mp;  // macroscopic output (interior, x fastest) or null
+};
+
+struct FillArgs {
+  Layout L;
+  void *f;               // state being filled (in place)
+  const uint32_t *mask;
+  int nxw;
+  int wall_y, wall_z;
+  const void *f_in;      // inlet equilibrium, Q stored elements (channel profile)
+};
+
+struct FaceOp {
+  int kind;  // 0 copy (inlet), 1 extrapolate (outlet), 2 bounce (wall)
+  int axis;  // 0 x, 1 y, 2 z
+  int side;  // 0 low, 1 high
+};
+
+struct LinkArgs {
+  Layout L;
+  void *f;
+  const int4 *links;     // (x, y, z, k): solid cell s, direction k, s + e_k fluid
+  long long n;
+  int reach;             // 1: halfway bounce-back, 2: the reference's s + 2 e_k rule
+  double *partials;      // 3 doubles per block
+  unsigned int *counter; // last-block detection, self-resetting
+  double *hist;          // force history, 3 doubles per slot
+  long long *step;       // device step counter (history slot = step % cap)
+  long long cap;
+};
+
+struct ReduceArgs {
+  Layout L;
+  const void *f;
+  const uint32_t *mask;
+  int nxw;
+  double *partials;      // 4 doubles per block
+  unsigned int *counter;
+  double *out;           // 4 doubles: mass, momentum x, y, z
+};
+
+// ---- launchers (defined in the .cu files, dispatch on lattice and storage) ----
+cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_fill_channel(int Q, int store, const FillArgs &a, cudaStream_t s);
+cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaStream_t s);
+cudaError_t launch_ghost_copy(int Q, int store, const Layout &L, const void *src, void *dst,
+                              cudaStream_t s);
+cudaError_t launch_links(int Q, int store, const LinkArgs &a, int blocks, cudaStream_t s);
+cudaError_t launch_init_macros(int Q, int store, const Layout &L, void *f, const double *u,
+                               const double *v, const double *w, const double *p,
+                               cudaStream_t s);
+cudaError_t launch_init_channel(int Q, int store, const Layout &L, void *f,
+                                const uint32_t *mask, int nxw, double u_in, double amp,
+                                unsigned long long seed, double *mu, double *mv, double *mw,
+                                double *mp, cudaStream_t s);
+cudaError_t launch_reduce_mass(int Q, int store, const ReduceArgs &a, int blocks,
+                               cudaStream_t s);
+cudaError_t launch_get_f(int Q, int store, const Layout &L, const void *f, double *out,
+                         cudaStream_t s);
+cudaError_t launch_set_f(int Q, int store, const Layout &L, void *f, const double *in,
+                         cudaStream_t s);
+cudaError_t launch_fill_value(int Q, int store, const Layout &L, void *f, cudaStream_t s);
+
+// Number of kernel launches issued through the launchers (all handles).
+long long launches();
+void count_launch(long long n = 1);
+
+// Perturbation of the initial u_y: amp * (2 r - 1), r from splitmix64 of
+// (seed + cell * golden ratio constant), 53 bits.
+__host__ __device__ inline unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+  return x ^ (x >> 31);
+}
+__host__ __device__ inline double perturbation(unsigned long long seed, long long cell,
+                                               double amp) {
+  unsigned long long r = splitmix64(seed + (unsigned long long)cell * 0x9E3779B97F4A7C15ULL);
+  double u01 = (double)(r >> 11) * (1.0 / 9007199254740992.0);
+  return amp * (2.0 * u01 - 1.0);
+}
+
+}  // namespace cflbm

@@ -1,0 +1,23 @@
+// D3Q27 instantiations of the fused sweep (see sweep.cuh).
+#include "sweep.cuh"
+
+namespace cflbm {
+
+cudaError_t launch_sweep_q27(int store, int compute, const SweepArgs &a, cudaStream_t s) {
+  if (compute == COMPUTE_F64) {
+    switch (store) {
+      case STORE_F64: return launch_sweep_t<27, double, double, 3>(a, s);
+      case STORE_F32: return launch_sweep_t<27, float, double, 3>(a, s);
+      case STORE_F16: return launch_sweep_t<27, F16Dev, double, 3>(a, s);
+    }
+  } else {
+    switch (store) {
+      case STORE_F64: return launch_sweep_t<27, double, float, 4>(a, s);
+      case STORE_F32: return launch_sweep_t<27, float, float, 4>(a, s);
+      case STORE_F16: return launch_sweep_t<27, F16Dev, float, 4>(a, s);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace cflbm

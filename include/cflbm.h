@@ -1,0 +1,189 @@
+/* cflbm.h -- C ABI of the GB300 lattice-Boltzmann cylinder-flow solver.
+ *
+ * One handle = one channel (or one reference-profile box) resident on one GPU,
+ * with its own CUDA stream.  Every call returns 0 on success or a CFLBM_E_* code;
+ * cflbm_last_error() gives the message of the last failure on the calling thread.
+ * Calls on one handle are not thread-safe; separate handles are independent.
+ *
+ * The entry points replace the per-step methods of the reference's solver class
+ * (Maccchiatooo/Cylinder-flow, "3D MPI+KOKKOS+MPIIO/lbm.hpp:106-233" and
+ * "MPI Kokkos/lbm.hpp:64-128"); each declaration names the reference code it
+ * stands in for.  Array arguments are plain host pointers unless a name says
+ * otherwise; field arrays cover the interior only, x fastest ("Fortran order"),
+ * the order the reference writes its Tecplot blocks in
+ * ("3D MPI+KOKKOS+MPIIO/lbm.cpp:444-460").
+ */
+#ifndef CFLBM_H
+#define CFLBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CFLBM_ABI_VERSION 1
+
+/* ---- error codes ---------------------------------------------------------- */
+#define CFLBM_OK 0
+#define CFLBM_E_INVALID 1     /* bad argument or configuration */
+#define CFLBM_E_CUDA 2        /* a CUDA runtime call failed */
+#define CFLBM_E_NOMEM 3       /* device or host allocation failed */
+#define CFLBM_E_NUMERIC 4     /* NaN/Inf detected in a checked quantity */
+#define CFLBM_E_IO 5          /* file I/O failed */
+#define CFLBM_E_UNSUPPORTED 6 /* combination not built */
+
+/* ---- enumerations ----------------------------------------------------------- */
+enum cflbm_lattice { CFLBM_D2Q9 = 9, CFLBM_D3Q27 = 27 };
+/* Population storage.  FP16DEV stores f_i / t_i (f_i is already the deviation
+ * from t_i*rho0, as in the reference) as IEEE binary16. */
+enum cflbm_storage { CFLBM_STORE_FP64 = 0, CFLBM_STORE_FP32 = 1, CFLBM_STORE_FP16DEV = 2 };
+/* Arithmetic of the collision. */
+enum cflbm_compute { CFLBM_COMPUTE_FP64 = 0, CFLBM_COMPUTE_FP32 = 1 };
+/* Boundary/initial-condition profile.
+ *  CHANNEL: the benchmark channel (equilibrium inlet, zero-gradient outlet,
+ *           free-slip/no-slip/periodic walls, halfway bounce-back on solids).
+ *  REF2D:   the reference's 2-D solver at one rank, "MPI Kokkos/lbm.cpp"
+ *           (Poiseuille inlet override, p = 0 outlet, its wall and solid rules,
+ *           disk of diameter 0.03125*(nx-1) at the box centre).
+ *  REF3D:   the reference's 3-D solver at one rank, "3D MPI+KOKKOS+MPIIO/lbm.cpp"
+ *           (sphere at ((nx-1)/8)^3, radius (nx-1)/64). */
+enum cflbm_profile { CFLBM_PROFILE_CHANNEL = 0, CFLBM_PROFILE_REF2D = 1, CFLBM_PROFILE_REF3D = 2 };
+enum cflbm_wall { CFLBM_WALL_FREESLIP = 0, CFLBM_WALL_NOSLIP = 1, CFLBM_WALL_PERIODIC = 2 };
+enum cflbm_geom { CFLBM_GEOM_NONE = 0, CFLBM_GEOM_CYLINDER = 1, CFLBM_GEOM_SPHERE = 2 };
+
+typedef struct cflbm_handle cflbm_handle;
+
+/* Construction parameters.  Fill with cflbm_config_default() first. */
+typedef struct cflbm_config {
+  int lattice;          /* CFLBM_D2Q9 or CFLBM_D3Q27 */
+  int nx, ny, nz;       /* interior cells (reference glx, gly, glz); nz = 1 in 2-D */
+  int storage;          /* enum cflbm_storage */
+  int compute;          /* enum cflbm_compute */
+  int profile;          /* enum cflbm_profile */
+  int wall_y, wall_z;   /* CHANNEL only: enum cflbm_wall for the y and z face pairs */
+  double tau0;          /* reference System::tau = u0*R/Re/cs2; omega = 1/(tau0+0.5) */
+  double u0;            /* CHANNEL: inlet speed; REF*: Poiseuille peak speed */
+  int geom;             /* CHANNEL: enum cflbm_geom */
+  double cx, cy, cz;    /* CHANNEL: body centre in cell coordinates */
+  double diam;          /* CHANNEL: body diameter in cells (Cd reference length) */
+  double perturb_amp;   /* CHANNEL: amplitude of the seeded uniform u_y perturbation */
+  uint64_t seed;        /* CHANNEL: perturbation seed */
+  const uint8_t *solid; /* CHANNEL: optional nx*ny*nz mask (1 = solid), overrides geom */
+  const double *alpha;  /* CHANNEL: optional nx*ny*nz Brinkman porosity in [0,1] */
+  const int32_t *ref_ran; /* REF*: the reference's per-node draw over the ghosted box
+                             (its layout, (i*ly+j)*lz+k), or NULL for a seeded draw */
+  int force_history;    /* capacity (steps) of the on-device force history; 0 = 65536 */
+  int device;           /* CUDA device ordinal */
+} cflbm_config;
+
+/* Geometry/step counters and device layout of a handle. */
+typedef struct cflbm_info {
+  int lattice, nx, ny, nz, storage, compute, profile;
+  int ghost;            /* ghost layers around the interior */
+  int pitch_x;          /* elements per padded x row */
+  int64_t pop_stride;   /* elements between populations */
+  int64_t steps_done;   /* time steps advanced since creation (or last set_f) */
+  int64_t n_links;      /* fluid->solid links (bounce-back, force) */
+  int64_t n_solid;      /* solid interior cells */
+  double omega;         /* 1/(tau0+0.5) */
+  double bytes_per_cell_step; /* algorithmic HBM bytes per cell update of the sweep */
+  size_t device_bytes;  /* device memory held by the handle */
+} cflbm_info;
+
+/* Defaults: D2Q9 64x32, FP64 storage and arithmetic, CHANNEL, free-slip y,
+ * periodic z, tau0 = 0.03, u0 = 0.05, no body, no perturbation. */
+int cflbm_config_default(cflbm_config *cfg);
+
+/* Allocate device state and initialise it (f = equilibrium of the initial
+ * macroscopic fields).  Replaces LBM::LBM + LBM::Initialize
+ * ("3D MPI+KOKKOS+MPIIO/lbm.hpp:146-219", "lbm.cpp:36-256";
+ * "MPI Kokkos/lbm.hpp:114", "lbm.cpp:47-126"). */
+int cflbm_create(const cflbm_config *cfg, cflbm_handle **out);
+
+/* Free everything the handle owns.  NULL is accepted. */
+int cflbm_destroy(cflbm_handle *h);
+
+/* Advance nsteps time steps.  One step = the reference's
+ * Collision(); [pack(); exchange(); unpack();] Streaming(); Update();
+ * ("3D MPI+KOKKOS+MPIIO/main.cpp:29-45", lbm.cpp:257-417;
+ * "MPI Kokkos/main.cpp:26-37", lbm.cpp:127-457), fused into one pull sweep plus
+ * a boundary kernel.  The halo exchange collapses to nothing at one rank.
+ * Asynchronous with respect to the host; errors of earlier launches surface here
+ * or at the next synchronising call. */
+int cflbm_step(cflbm_handle *h, int nsteps);
+
+/* Block until all work queued on the handle's stream has finished. */
+int cflbm_synchronize(cflbm_handle *h);
+
+/* Macroscopic fields after the last step: u, v, w, p over the interior, x
+ * fastest, as LBM::Update leaves them ("3D.../lbm.cpp:374-417": p = sum f/3,
+ * u = sum f e, zero in solids, reference-profile inlet/outlet overrides).
+ * Any pointer may be NULL.  Host pointers; synchronises. */
+int cflbm_macros(cflbm_handle *h, double *u, double *v, double *w, double *p);
+
+/* Same, into device pointers (no synchronisation; ordered on the handle's
+ * stream). */
+int cflbm_macros_device(cflbm_handle *h, double *d_u, double *d_v, double *d_w, double *d_p);
+
+/* Momentum-exchange force of the last step and its coefficients.  Replaces the
+ * force block of "MPI Kokkos/lbm.cpp:356-407": fxyz = (Fx, Fy, Fz) in lattice
+ * units, cd_cl = (2 Fx / (u0^2 A), 2 Fy / (u0^2 A)) with A the reference area
+ * (2-D: D; spanwise cylinder: D*nz; sphere: pi D^2/4; REF2D: D = 0.03125*(nx-1)).
+ * Either pointer may be NULL.  Synchronises. */
+int cflbm_forces(cflbm_handle *h, double fxyz[3], double cd_cl[2]);
+
+/* Per-step force history (Fx, Fy, Fz per step, oldest first) of the last
+ * min(steps_done, capacity) steps.  Writes up to max_steps rows into out
+ * (3*max_steps doubles) and the row count into *n_out.  Synchronises. */
+int cflbm_force_history(cflbm_handle *h, double *out, int64_t max_steps, int64_t *n_out);
+
+/* Domain sums in FP64: mass = sum over fluid cells of (1 + sum_i f_i)
+ * (i.e. rho), and momentum (3 doubles).  Either pointer may be NULL. */
+int cflbm_mass(cflbm_handle *h, double *mass, double momentum[3]);
+
+/* Dump / restore the post-collision populations of the interior in FP64,
+ * layout [i][z][y][x] (x fastest), q*nx*ny*nz doubles.  The reference has no
+ * restart; this is the checkpoint path.  set_f also sets steps_done. */
+int cflbm_get_f(cflbm_handle *h, double *out);
+int cflbm_set_f(cflbm_handle *h, const double *in, int64_t steps_done);
+
+/* Handle geometry, counters and memory. */
+int cflbm_get_info(cflbm_handle *h, cflbm_info *info);
+
+/* Write the Tecplot binary file of LBM::MPIoutput(n)
+ * ("3D MPI+KOKKOS+MPIIO/lbm.cpp:419-739"; 2-D: "MPI Kokkos/lbm.cpp:459-737"):
+ * "#!TDV112" header with variables x,y,(z,)u,v,(w,)p, zone "ZONE 001", solution
+ * time n, min/max of every variable, then the variables as x-fastest FP64
+ * blocks.  Byte-identical to the reference's file for the same fields. */
+int cflbm_write_tecplot(cflbm_handle *h, const char *path, int n);
+
+/* The same writer for caller-supplied host fields (dim 2: u, v, p used, w
+ * ignored; nz ignored).  Needs no GPU. */
+int cflbm_write_tecplot_fields(const char *path, int dim, int nx, int ny, int nz,
+                               const double *u, const double *v, const double *w,
+                               const double *p, int n);
+
+/* The CUDA stream (cudaStream_t) the handle launches on, for callers that
+ * order their own work or events against the solver. */
+int cflbm_get_stream(cflbm_handle *h, void **stream);
+
+/* Kernel timing: when enabled, CUDA events are recorded on the handle's stream
+ * around every sweep launch and around every boundary phase (ghost fill +
+ * bounce-back/force).  cflbm_get_timing synchronises and returns
+ * ms[0] = total sweep time, ms[1] = total boundary time, counts[0] = sweeps,
+ * counts[1] = boundary phases since the last reset, then resets. */
+int cflbm_set_timing(cflbm_handle *h, int enable);
+int cflbm_get_timing(cflbm_handle *h, double ms[2], int64_t counts[2]);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *cflbm_last_error(void);
+
+/* Number of kernel launches issued by this library since load (all handles). */
+int64_t cflbm_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFLBM_H */

@@ -1,0 +1,116 @@
+"""C ABI library: loads, exports every declared entry point, validates input,
+and writes the reference's Tecplot bytes (all without a GPU)."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, load_golden
+
+import cflbm
+from cflbm import _lib as C
+from cflbm.solver import write_tecplot_fields
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_0-9]+\s*\**\s*(cflbm_\w+)\s*\(",
+                                    txt, re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    names = declared_symbols()
+    assert len(names) >= 17
+    out = subprocess.run(["nm", "-D", "--defined-only", C.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(cflbm_\w+)", out))
+    missing = names - exported
+    assert not missing, missing
+    for n in names:
+        assert hasattr(C.lib, n)
+    # every declared symbol has a ctypes signature in the binding
+    assert names <= set(C.SIGNATURES)
+
+
+def test_build_targets_sm103a_only():
+    from cflbm import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_config_default():
+    cfg = C.Config()
+    assert C.lib.cflbm_config_default(ctypes.byref(cfg)) == 0
+    assert cfg.lattice == 9 and cfg.nx == 64 and cfg.ny == 32
+    assert cfg.storage == C.STORE_FP64 and cfg.compute == C.COMPUTE_FP64
+    assert cfg.tau0 == 0.03 and cfg.u0 == 0.05
+
+
+@pytest.mark.parametrize("field,value", [("lattice", 7), ("nx", 2), ("storage", 9),
+                                         ("compute", 5), ("profile", 4), ("wall_y", 3),
+                                         ("tau0", -0.6), ("force_history", -1)])
+def test_create_rejects_bad_config_before_touching_the_gpu(field, value):
+    cfg = C.Config()
+    C.lib.cflbm_config_default(ctypes.byref(cfg))
+    setattr(cfg, field, value)
+    h = ctypes.c_void_p()
+    rc = C.lib.cflbm_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert rc == 1
+    assert not h.value
+    assert C.lib.cflbm_last_error()
+
+
+def test_profile_lattice_mismatch_rejected():
+    cfg = C.Config()
+    C.lib.cflbm_config_default(ctypes.byref(cfg))
+    cfg.profile = C.PROFILE_REF3D
+    h = ctypes.c_void_p()
+    assert C.lib.cflbm_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert b"REF3D" in C.lib.cflbm_last_error()
+
+
+def test_null_handle_calls_fail_cleanly():
+    assert C.lib.cflbm_step(None, 1) == 1
+    assert C.lib.cflbm_destroy(None) == 0
+    with pytest.raises(cflbm.CflbmError):
+        C.check(C.lib.cflbm_synchronize(None), "cflbm_synchronize")
+
+
+def test_tecplot_2d_bytes_match_reference(tmp_path):
+    g = load_golden("ref2d_96x40")
+    path = str(tmp_path / "out.plt")
+    write_tecplot_fields(path, g["u"], g["v"], None, g["p"], 1)
+    ref = open(os.path.join(GOLDEN, "ref2d_96x40_output1.plt"), "rb").read()
+    assert open(path, "rb").read() == ref
+
+
+def test_tecplot_3d_bytes_match_reference(tmp_path):
+    g = load_golden("ref3d_40x12x12")
+    path = str(tmp_path / "out.plt")
+    write_tecplot_fields(path, g["u"], g["v"], g["w"], g["p"], 1)
+    ref = open(os.path.join(GOLDEN, "ref3d_40x12x12_output1.plt"), "rb").read()
+    mine = open(path, "rb").read()
+    assert len(mine) == len(ref) == 332 + 7 * 8 * 40 * 12 * 12
+    assert mine == ref
+
+
+def test_strouhal_of_a_pure_tone():
+    n, period = 4000, 200.0
+    t = np.arange(n)
+    cl = 0.3 * np.sin(2 * np.pi * t / period) + 1e-3 * t / n
+    st = cflbm.analysis.strouhal(cl, diam=20.0, u0=0.05)
+    assert abs(st - 20.0 / period / 0.05) < 2e-3
+
+
+def test_test_dat_format(tmp_path):
+    p = str(tmp_path / "test.dat")
+    cflbm.analysis.write_test_dat(p, np.array([[1.25, -0.5]]), append=False)
+    assert open(p).read() == "1.25000000000000000 -0.50000000000000000\n"
