@@ -165,8 +165,9 @@ def time_device(solver, steps, warmup):
     return e0.elapsed_time(e1)  # ms
 
 
-def variant_mlups(cflbm, local, storage, compute, steps, warmup):
-    with cflbm.Solver(device=local, storage=storage, compute=compute, **WORKLOAD) as s:
+def variant_mlups(cflbm, local, storage, compute, layout, steps, warmup):
+    with cflbm.Solver(device=local, storage=storage, compute=compute, layout=layout,
+                      **WORKLOAD) as s:
         ms = time_device(s, steps, warmup)
         s.set_timing(True)
         s.step(max(steps // 4, 3))
@@ -196,6 +197,9 @@ def run_gb300(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         with ClockSampler(local) as clk:
+            s.step(warmup)  # keep the GPU busy while the sampler starts
+            time.sleep(0.3)
+            s.synchronize()
             n_launch0 = cflbm.launch_count()
             e0.record(stream)
             s.step(steps)
@@ -221,9 +225,14 @@ def run_gb300(args):
     # ---- the other storage/arithmetic forms at the same grid ---------------------
     extra = {}
     if not args.quick:
-        for name, st, cp in (("fp64_arith", "fp64", "fp64"), ("fp32_store", "fp32", "fp32"),
-                             ("fp16dev_store", "fp16dev", "fp32")):
-            v = variant_mlups(cflbm, local, st, cp, max(steps // 3, 20) if cp == "fp64" else steps,
+        for name, st, cp, lay in (("fp64_arith", "fp64", "fp64", "soa"),
+                                  ("fp64_store_rows", "fp64", "fp32", "rows"),
+                                  ("fp32_store", "fp32", "fp32", "soa"),
+                                  ("fp32_store_rows", "fp32", "fp32", "rows"),
+                                  ("fp16dev_store", "fp16dev", "fp32", "soa"),
+                                  ("fp16dev_store_rows", "fp16dev", "fp32", "rows")):
+            v = variant_mlups(cflbm, local, st, cp, lay,
+                              max(steps // 5, 20) if cp == "fp64" else steps // 2,
                               min(warmup, 5))
             v["hbm_frac"] = v["bytes_per_cell"] * CELLS / (v["sweep_us"] * 1e-6) / 1e9 / peak
             extra[name] = {k: round(x, 4) if isinstance(x, float) else x for k, x in v.items()}
@@ -339,19 +348,51 @@ def run_reference(args):
     return 0
 
 
+def run_profile(args):
+    """A bare stepping loop for profiler captures (no extras, no CPU baseline)."""
+    import cflbm
+    wl = dict(WORKLOAD, nx=args.nx, ny=args.ny, nz=args.nz, cx=args.nx / 4.0, cy=args.ny / 2.0)
+    with cflbm.Solver(storage=args.storage, compute=args.compute, layout=args.layout,
+                      **wl) as s:
+        s.step(args.warmup)
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.step(args.steps)
+        s.synchronize()
+        dt = time.perf_counter() - t0
+        info = s.info()
+    cells = args.nx * args.ny * args.nz
+    print(json.dumps({"profile_case": [args.nx, args.ny, args.nz], "storage": args.storage,
+                      "compute": args.compute, "steps": args.steps,
+                      "mlups_wall": cells * args.steps / dt / 1e6,
+                      "bytes_per_cell": info.bytes_per_cell_step,
+                      "device_bytes": info.device_bytes}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline variant only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--profile", action="store_true",
+                    help="bare stepping loop on an --nx/--ny/--nz grid for profiler captures")
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--ny", type=int, default=NY)
+    ap.add_argument("--nz", type=int, default=NZ)
+    ap.add_argument("--storage", default="fp64", choices=["fp64", "fp32", "fp16dev"])
+    ap.add_argument("--compute", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--layout", default="soa", choices=["soa", "rows"])
     args = ap.parse_args()
     args.steps_ref = 1
     if args.warmup < 3:
         args.warmup = 3
+    if args.profile:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

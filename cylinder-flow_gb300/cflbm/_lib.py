@@ -18,6 +18,7 @@ COMPUTE_FP64, COMPUTE_FP32 = 0, 1
 PROFILE_CHANNEL, PROFILE_REF2D, PROFILE_REF3D = 0, 1, 2
 WALL_FREESLIP, WALL_NOSLIP, WALL_PERIODIC = 0, 1, 2
 GEOM_NONE, GEOM_CYLINDER, GEOM_SPHERE = 0, 1, 2
+LAYOUT_SOA, LAYOUT_ROWS = 0, 1
 
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "numeric error",
           5: "I/O error", 6: "unsupported"}
@@ -35,7 +36,7 @@ class Config(ctypes.Structure):
         ("diam", ctypes.c_double), ("perturb_amp", ctypes.c_double),
         ("seed", ctypes.c_uint64), ("solid", ctypes.POINTER(ctypes.c_uint8)),
         ("alpha", _dp), ("ref_ran", ctypes.POINTER(ctypes.c_int32)),
-        ("force_history", ctypes.c_int), ("device", ctypes.c_int),
+        ("force_history", ctypes.c_int), ("device", ctypes.c_int), ("layout", ctypes.c_int),
     ]
 
 
@@ -47,6 +48,7 @@ class Info(ctypes.Structure):
         ("pop_stride", ctypes.c_int64), ("steps_done", ctypes.c_int64),
         ("n_links", ctypes.c_int64), ("n_solid", ctypes.c_int64), ("omega", ctypes.c_double),
         ("bytes_per_cell_step", ctypes.c_double), ("device_bytes", ctypes.c_size_t),
+        ("layout", ctypes.c_int),
     ]
 
 

@@ -33,6 +33,7 @@ class Solver:
         "wall_z": {"freeslip": C.WALL_FREESLIP, "noslip": C.WALL_NOSLIP,
                    "periodic": C.WALL_PERIODIC},
         "geom": {"none": C.GEOM_NONE, "cylinder": C.GEOM_CYLINDER, "sphere": C.GEOM_SPHERE},
+        "layout": {"soa": C.LAYOUT_SOA, "rows": C.LAYOUT_ROWS},
     }
 
     def __init__(self, **kw):

@@ -57,6 +57,7 @@ void free_handle(cflbm_handle *h) {
   if (h->cfg.device >= 0) cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
+                  h->d_near, h->d_tile_slow, h->d_slow_tiles,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
                   h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
   for (void *p : ptrs)
@@ -100,6 +101,47 @@ void build_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
           links.push_back(make_int4(x, y, z, k));
         }
       }
+}
+
+// Cells that are solid or have a solid neighbour (any lattice direction).
+template <int Q>
+std::vector<uint8_t> near_solid(const std::vector<uint8_t> &solid, int nx, int ny, int nz) {
+  using L = Lat<Q>;
+  std::vector<uint8_t> nr(solid.size(), 0);
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const size_t n = ((size_t)z * ny + y) * nx + x;
+        if (solid[n]) { nr[n] = 1; continue; }
+        for (int k = 1; k < Q; ++k) {
+          const int X = x + L::ex(k), Y = y + L::ey(k), Z = z + L::ez(k);
+          if (X < 0 || X >= nx || Y < 0 || Y >= ny || Z < 0 || Z >= nz) continue;
+          if (solid[((size_t)Z * ny + Y) * nx + X]) { nr[n] = 1; break; }
+        }
+      }
+  return nr;
+}
+
+// Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) that the
+// channel sweep must resolve: on a y or z face, or holding a cell that is solid
+// or next to a solid.  Returns the per-tile flags and fills the list.
+std::vector<unsigned char> slow_tiles(const std::vector<uint8_t> &nr, int nx, int ny, int nz,
+                                      int nxw, bool d3, std::vector<int> &list) {
+  std::vector<unsigned char> flag((size_t)nxw * ny * nz, 0);
+  list.clear();
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int w = 0; w < nxw; ++w) {
+        bool slow = y == 0 || y == ny - 1 || (d3 && (z == 0 || z == nz - 1));
+        for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !slow; ++x)
+          if (nr[((size_t)z * ny + y) * nx + x]) slow = true;
+        if (slow) {
+          const size_t t = ((size_t)z * ny + y) * nxw + w;
+          flag[t] = 1;
+          list.push_back((int)t);
+        }
+      }
+  return flag;
 }
 
 // Equilibrium of the channel inlet (p = 0, u = (u_in, 0, 0)) in storage format.
@@ -151,6 +193,8 @@ int validate(const cflbm_config *c) {
     return fail(CFLBM_E_INVALID, "tau0 = %g gives omega outside (0, 2)", c->tau0);
   if (!std::isfinite(c->u0)) return fail(CFLBM_E_INVALID, "u0 is not finite");
   if (c->force_history < 0) return fail(CFLBM_E_INVALID, "force_history < 0");
+  if (c->layout != CFLBM_LAYOUT_SOA && c->layout != CFLBM_LAYOUT_ROWS)
+    return fail(CFLBM_E_INVALID, "layout %d unknown", c->layout);
   return CFLBM_OK;
 }
 
@@ -217,7 +261,15 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   L.px = ((align + nx + G + 4 + align - 1) / align) * align;
   L.nyp = ny + 2 * G;
   L.nzp = nz + 2 * L.Gz;
-  L.S = (long long)L.px * L.nyp * L.nzp;
+  if (cfg->layout == CFLBM_LAYOUT_ROWS) {
+    L.S = L.px;
+    L.rs = (long long)Q * L.px;
+  } else {
+    L.S = (long long)L.px * L.nyp * L.nzp;
+    L.rs = L.px;
+  }
+  L.zs = L.rs * L.nyp;
+  L.total = (long long)Q * L.px * L.nyp * L.nzp;
   h->nxw = (nx + 31) / 32;
   h->omega = 1.0 / (cfg->tau0 + 0.5);
   if (!(h->omega > 0.0 && h->omega < 2.0))
@@ -249,7 +301,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
 
   // Device allocations.
   const size_t N = (size_t)nx * ny * nz;
-  h->f_bytes = (size_t)Q * L.S * es;
+  h->f_bytes = (size_t)L.total * es;
   if ((rc = dev_alloc(h, &h->fA, h->f_bytes))) return rc;
   if ((rc = dev_alloc(h, &h->fB, h->f_bytes))) return rc;
   CK_CUDA(cudaMemsetAsync(h->fA, 0, h->f_bytes, h->stream));
@@ -271,8 +323,35 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaMemsetAsync(h->d_step, 0, sizeof(long long), h->stream));
   h->link_blocks = (int)std::min<long long>(std::max<long long>((h->n_links + 255) / 256, 1), 1024);
   h->reduce_blocks = (int)std::min<long long>(std::max<long long>(((long long)N + 255) / 256, 1), 2048);
-  if ((rc = dev_alloc_t(h, &h->d_partials, 4 * (size_t)std::max(h->link_blocks, h->reduce_blocks))))
-    return rc;
+  if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
+    const std::vector<uint8_t> nr = d3 ? near_solid<27>(solid, nx, ny, nz)
+                                       : near_solid<9>(solid, nx, ny, nz);
+    const std::vector<uint32_t> nearw = pack_mask(nr, nx, ny, nz, h->nxw);
+    if ((rc = dev_alloc_t(h, &h->d_near, nearw.size()))) return rc;
+    CK_CUDA(cudaMemcpyAsync(h->d_near, nearw.data(), nearw.size() * 4, cudaMemcpyHostToDevice,
+                            h->stream));
+    std::vector<int> list;
+    const std::vector<unsigned char> flag = slow_tiles(nr, nx, ny, nz, h->nxw, d3, list);
+    h->n_slow = (int)list.size();
+    if ((rc = dev_alloc_t(h, &h->d_tile_slow, flag.size()))) return rc;
+    CK_CUDA(cudaMemcpyAsync(h->d_tile_slow, flag.data(), flag.size(), cudaMemcpyHostToDevice,
+                            h->stream));
+    if ((rc = dev_alloc_t(h, &h->d_slow_tiles, list.size() + 1))) return rc;
+    if (!list.empty())
+      CK_CUDA(cudaMemcpyAsync(h->d_slow_tiles, list.data(), list.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, h->stream));
+    CK_CUDA(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < Q; ++i) {
+      const int ex = d3 ? Lat<27>::ex(i) : Lat<9>::ex(i);
+      const double w = d3 ? Lat<27>::w(i) : Lat<9>::w(i);
+      const double edu = ex * cfg->u0;
+      h->f_in[i] = w * 0.0 * 3.0 + w * (3.0 * edu + 4.5 * edu * edu - 1.5 * cfg->u0 * cfg->u0);
+    }
+    CK_CUDA(cudaStreamSynchronize(h->stream));  // host vectors die at scope end
+  }
+  const size_t nparts = std::max<size_t>(4 * (size_t)std::max(h->link_blocks, h->reduce_blocks),
+                                         3 * (size_t)std::max((h->n_slow + SLOW_TILES_PER_BLOCK - 1) / SLOW_TILES_PER_BLOCK, 1));
+  if ((rc = dev_alloc_t(h, &h->d_partials, nparts))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_counter, 1))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_counter2, 1))) return rc;
   CK_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(unsigned), h->stream));
@@ -292,8 +371,8 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
       CK_CUDA(cudaStreamSynchronize(h->stream));
     }
     CK_CUDA(launch_init_channel(Q, cfg->storage, L, h->fA, h->d_mask, h->nxw, cfg->u0,
-                                cfg->perturb_amp, cfg->seed, h->d_mu, h->d_mv, h->d_mw,
-                                h->d_mp, h->stream));
+                                cfg->perturb_amp, cfg->seed, h->d_alpha, h->omega, h->d_mu,
+                                h->d_mv, h->d_mw, h->d_mp, h->stream));
   } else {
     if ((rc = dev_alloc_t(h, &h->d_inlet, ref.inlet.size()))) return rc;
     CK_CUDA(cudaMemcpyAsync(h->d_inlet, ref.inlet.data(), ref.inlet.size() * 8,
@@ -357,7 +436,8 @@ static int record_event(cflbm_handle *h, size_t *idx) {
 static int one_step(cflbm_handle *h, bool write_macros) {
   size_t tb0 = 0, tb1 = 0, ts0 = 0, ts1 = 0;
   int trc;
-  if (h->timing && (trc = record_event(h, &tb0))) return trc;
+  if (h->timing && h->cfg.profile != CFLBM_PROFILE_CHANNEL && (trc = record_event(h, &tb0)))
+    return trc;
   const int Q = h->Q;
   const int st = h->cfg.storage;
   const Layout &L = h->L;
@@ -371,8 +451,44 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   fa.f_in = h->d_fin;
   const bool ref = h->cfg.profile != CFLBM_PROFILE_CHANNEL;
   if (!ref) {
-    CK_CUDA(launch_fill_channel(Q, st, fa, h->stream));
-  } else if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
+    SweepArgs sa{};
+    sa.L = L;
+    sa.fa = h->fA;
+    sa.fb = h->fB;
+    sa.mask = h->d_mask;
+    sa.nxw = h->nxw;
+    sa.omega = h->omega;
+    sa.omega_f = (float)h->omega;
+    sa.alpha = h->d_alpha;
+    if (write_macros) {
+      sa.mu = h->d_mu;
+      sa.mv = h->d_mv;
+      sa.mw = h->d_mw;
+      sa.mp = h->d_mp;
+    }
+    sa.near = h->d_near;
+    sa.wall_y = h->cfg.wall_y;
+    sa.wall_z = h->cfg.wall_z;
+    for (int i = 0; i < Q; ++i) sa.f_in[i] = h->f_in[i];
+    sa.tile_slow = h->d_tile_slow;
+    sa.slow_tiles = h->d_slow_tiles;
+    sa.n_slow = h->n_slow;
+    sa.partials = h->d_partials;
+    sa.counter = h->d_counter;
+    sa.hist = h->d_hist;
+    sa.step = h->d_step;
+    sa.cap = h->hist_cap;
+    if (h->timing && (trc = record_event(h, &ts0))) return trc;
+    CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream));
+    if (h->timing) {
+      if ((trc = record_event(h, &ts1))) return trc;
+      h->sweep_ev.push_back({ts0, ts1});
+    }
+    std::swap(h->fA, h->fB);
+    ++h->steps_done;
+    return CFLBM_OK;
+  }
+  if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
     // "MPI Kokkos/lbm.cpp:315-345": inlet, outlet, then the two wall rows.
     const FaceOp ops[4] = {{0, 0, 0}, {1, 0, 1}, {2, 1, 0}, {2, 1, 1}};
     for (const FaceOp &op : ops) CK_CUDA(launch_face_op(Q, st, fa, op, h->stream));
@@ -585,6 +701,7 @@ int cflbm_get_info(cflbm_handle *h, cflbm_info *info) {
   info->ghost = h->L.G;
   info->pitch_x = h->L.px;
   info->pop_stride = h->L.S;
+  info->layout = h->cfg.layout;
   info->steps_done = h->steps_done;
   info->n_links = h->n_links;
   info->n_solid = h->n_solid;

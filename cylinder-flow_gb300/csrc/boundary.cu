@@ -211,13 +211,15 @@ __global__ void ghost_copy_kernel(const Layout L, const void *src_, void *dst_) 
   using E = typename Store<ST>::elem;
   const E *src = static_cast<const E *>(src_);
   E *dst = static_cast<E *>(dst_);
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.S;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(e % L.px) - L.xoff;
-    const long long r = e / L.px;
+  const long long cells = (long long)L.px * L.nyp * L.nzp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < cells;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % L.px) - L.xoff;
+    const long long r = t / L.px;
     const int y = (int)(r % L.nyp) - L.G;
     const int z = (int)(r / L.nyp) - L.Gz;
     if (L.interior(x, y, z)) continue;
+    const long long e = L.idx(x, y, z);
 #pragma unroll 9
     for (int i = 0; i < Q; ++i) dst[i * L.S + e] = src[i * L.S + e];
   }
@@ -318,6 +320,7 @@ __global__ void init_macros_kernel(const Layout L, void *f_, const double *u, co
 template <int Q, class ST>
 __global__ void init_channel_kernel(const Layout L, void *f_, const uint32_t *mask, int nxw,
                                     double u_in, double amp, unsigned long long seed,
+                                    const float *alpha, double omega,
                                     double *mu, double *mv, double *mw, double *mp) {
   using E = typename Store<ST>::elem;
   E *f = static_cast<E *>(f_);
@@ -335,12 +338,22 @@ __global__ void init_channel_kernel(const Layout L, void *f_, const uint32_t *ma
     mw[t] = 0.0;
     mp[t] = 0.0;
     const long long c = L.idx(x, y, z);
+    // The state is post-collision: the first collision relaxes f = feq(u) toward
+    // feq((1 - alpha) u), the identity without porosity.
+    const double s = alpha ? 1.0 - (double)alpha[t] : 1.0;
     for (int i = 0; i < Q; ++i) {
       const double edu = DT<Q>::ex(i) * uu + DT<Q>::ey(i) * vv;
       const double udu = uu * uu + vv * vv;
-      const double feq = Lat<Q>::w(i) * 0.0 * 3.0 +
-                         Lat<Q>::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * udu);
-      f[i * L.S + c] = Dec<ST>::template put<Q>(feq, i);
+      const double f0 = Lat<Q>::w(i) * 0.0 * 3.0 +
+                        Lat<Q>::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * udu);
+      double fp = f0;
+      if (alpha) {
+        const double eb = s * edu, ub = s * s * udu;
+        const double fb = Lat<Q>::w(i) * 0.0 * 3.0 +
+                          Lat<Q>::w(i) * (3.0 * eb + 4.5 * eb * eb - 1.5 * ub);
+        fp = f0 - (f0 - fb) * omega;
+      }
+      f[i * L.S + c] = Dec<ST>::template put<Q>(fp, i);
     }
   }
 }
@@ -445,6 +458,15 @@ cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cuda
   return Q == 9 ? launch_sweep_q9(store, compute, a, s) : launch_sweep_q27(store, compute, a, s);
 }
 
+cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_sweep_channel_q27(int store, int compute, const SweepArgs &a, cudaStream_t s);
+
+cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
+                                 cudaStream_t s) {
+  return Q == 9 ? launch_sweep_channel_q9(store, compute, a, s)
+                : launch_sweep_channel_q27(store, compute, a, s);
+}
+
 // Dispatch helper: run F<Q, ST> for the runtime (Q, store).
 #define CFLBM_DISPATCH(Q, store, CALL)                                   \
   do {                                                                   \
@@ -484,7 +506,7 @@ cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaS
 
 cudaError_t launch_ghost_copy(int Q, int store, const Layout &L, const void *src, void *dst,
                               cudaStream_t s) {
-  const int blocks = blocks_for(L.S, 256);
+  const int blocks = blocks_for((long long)L.px * L.nyp * L.nzp, 256);
   CFLBM_DISPATCH(Q, store, (ghost_copy_kernel<QQ, ST><<<blocks, 256, 0, s>>>(L, src, dst)));
   count_launch();
   return cudaGetLastError();
@@ -510,12 +532,12 @@ cudaError_t launch_init_macros(int Q, int store, const Layout &L, void *f, const
 
 cudaError_t launch_init_channel(int Q, int store, const Layout &L, void *f,
                                 const uint32_t *mask, int nxw, double u_in, double amp,
-                                unsigned long long seed, double *mu, double *mv, double *mw,
-                                double *mp, cudaStream_t s) {
+                                unsigned long long seed, const float *alpha, double omega,
+                                double *mu, double *mv, double *mw, double *mp, cudaStream_t s) {
   const int blocks = blocks_for((long long)L.nx * L.ny * L.nz, 256);
   CFLBM_DISPATCH(Q, store,
                  (init_channel_kernel<QQ, ST><<<blocks, 256, 0, s>>>(
-                     L, f, mask, nxw, u_in, amp, seed, mu, mv, mw, mp)));
+                     L, f, mask, nxw, u_in, amp, seed, alpha, omega, mu, mv, mw, mp)));
   count_launch();
   return cudaGetLastError();
 }

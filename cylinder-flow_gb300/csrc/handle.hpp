@@ -17,6 +17,11 @@ struct cflbm_handle {
   void *fA = nullptr, *fB = nullptr;
   size_t f_bytes = 0;
   uint32_t *d_mask = nullptr;
+  uint32_t *d_near = nullptr;   // solid or next to solid (channel sweep slow path)
+  unsigned char *d_tile_slow = nullptr;  // per warp tile: needs the resolving kernel
+  int *d_slow_tiles = nullptr;           // list of those tiles
+  int n_slow = 0;
+  double f_in[27] = {0};        // inlet equilibrium (channel profile)
   int4 *d_links = nullptr;
   long long n_links = 0;
   long long n_solid = 0;

@@ -1,13 +1,17 @@
 // Internal device-side declarations of the cylinder-flow solver.
 //
-// Data layout in HBM (one array per population buffer, two buffers A/B):
-//   f[i][z + Gz][y + G][x + xoff]  (structure of arrays, x fastest)
-// with i the population, G ghost layers around the interior in x and y (and z in
-// 3-D), rows padded to `px` elements so every interior row starts on a 128-byte
-// boundary.  A holds the post-collision populations of the current step; the
-// sweep pulls from A and writes the next post-collision state into B; the
-// buffers then swap.  The ghost layers and the populations of solid cells that
-// face fluid are refilled before each sweep by the boundary kernels.
+// Data layout in HBM (two population buffers A/B, x fastest everywhere):
+//   SOA : f[i][z + Gz][y + G][x + xoff]   one array per population
+//   ROWS: f[z + Gz][y + G][i][x + xoff]   the Q rows of one (y, z) are adjacent
+// with G ghost layers around the interior in x and y (and z in 3-D) and rows
+// padded to `px` elements so every interior row starts on a 128-byte boundary.
+// In both layouts population i of cell (x, y, z) sits at i*S + idx(x, y, z) and
+// the pull source x - e_i is a constant offset, so each population is a pure
+// shift and every element is read exactly once per sweep.  ROWS keeps the 2Q
+// streams a warp touches within a few rows, i.e. a few DRAM pages and TLB
+// entries, instead of 2Q arrays hundreds of megabytes apart.
+// A holds the post-collision populations of the current step; the sweep pulls
+// from A and writes the next post-collision state into B; the buffers swap.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -19,6 +23,7 @@ enum Profile { PROFILE_CHANNEL = 0, PROFILE_REF2D = 1, PROFILE_REF3D = 2 };
 enum Wall { WALL_FREESLIP = 0, WALL_NOSLIP = 1, WALL_PERIODIC = 2 };
 enum StoreKind { STORE_F64 = 0, STORE_F32 = 1, STORE_F16 = 2 };
 enum ComputeKind { COMPUTE_F64 = 0, COMPUTE_F32 = 1 };
+enum LayoutKind { LAYOUT_SOA = 0, LAYOUT_ROWS = 1 };
 
 struct Layout {
   int nx, ny, nz;  // interior cells (nz = 1 in 2-D)
@@ -26,12 +31,15 @@ struct Layout {
   int xoff;        // element offset of interior x = 0 inside a row
   int px;          // row pitch in elements
   int nyp, nzp;    // padded y and z extents
-  long long S;     // elements per population
+  long long S;     // elements between populations of one cell
+  long long rs;    // elements between rows (y)
+  long long zs;    // elements between planes (z)
+  long long total; // elements per buffer
   __host__ __device__ long long idx(int x, int y, int z) const {
-    return ((long long)(z + Gz) * nyp + (y + G)) * px + (x + xoff);
+    return (long long)(z + Gz) * zs + (long long)(y + G) * rs + (x + xoff);
   }
   __host__ __device__ long long off(int ex, int ey, int ez) const {
-    return (long long)ex + (long long)px * ((long long)ey + (long long)nyp * ez);
+    return (long long)ex + rs * ey + zs * ez;
   }
   __host__ __device__ bool interior(int x, int y, int z) const {
     return x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz;
@@ -54,6 +62,18 @@ struct SweepArgs {
   const double *inlet_u; // ny*nz inlet velocity profile (reference profiles)
   const float *alpha;    // nx*ny*nz Brinkman porosity or null
   double *mu, *mv, *mw, *mp;  // macroscopic output (interior, x fastest) or null
+  // Channel profile (boundaries resolved inside the sweep):
+  const uint32_t *near;  // bit-packed: cell is solid or has a solid neighbour
+  int wall_y, wall_z;
+  double f_in[27];       // inlet equilibrium populations (p = 0, u = (u_in, 0, 0))
+  const unsigned char *tile_slow;  // per warp tile (32 cells of a row): 1 = resolve
+  const int *slow_tiles; // list of resolving tiles (tile = (z*ny + y)*nxw + x/32)
+  int n_slow;            // length of the list
+  double *partials;      // 3 doubles per block of the resolving kernel
+  unsigned int *counter; // finished force blocks (self-resetting)
+  double *hist;          // force history, 3 doubles per step
+  long long *step;       // device step counter (history slot = step % cap)
+  long long cap;
 };
 
 struct FillArgs {
@@ -96,6 +116,12 @@ struct ReduceArgs {
 
 // ---- launchers (defined in the .cu files, dispatch on lattice and storage) ----
 cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
+                                 cudaStream_t s);
+// Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z;
+// the resolving channel kernel runs 4 warp tiles per block.
+constexpr int SWEEP_BX = 32, SWEEP_BY = 4;
+constexpr int SLOW_TILES_PER_BLOCK = 4;
 cudaError_t launch_fill_channel(int Q, int store, const FillArgs &a, cudaStream_t s);
 cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaStream_t s);
 cudaError_t launch_ghost_copy(int Q, int store, const Layout &L, const void *src, void *dst,
@@ -106,8 +132,8 @@ cudaError_t launch_init_macros(int Q, int store, const Layout &L, void *f, const
                                cudaStream_t s);
 cudaError_t launch_init_channel(int Q, int store, const Layout &L, void *f,
                                 const uint32_t *mask, int nxw, double u_in, double amp,
-                                unsigned long long seed, double *mu, double *mv, double *mw,
-                                double *mp, cudaStream_t s);
+                                unsigned long long seed, const float *alpha, double omega,
+                                double *mu, double *mv, double *mw, double *mp, cudaStream_t s);
 cudaError_t launch_reduce_mass(int Q, int store, const ReduceArgs &a, int blocks,
                                cudaStream_t s);
 cudaError_t launch_get_f(int Q, int store, const Layout &L, const void *f, double *out,

@@ -1,87 +1,41 @@
 // The fused collide-and-stream sweep: one pass over the interior per time step.
 //
-// For every interior cell x the kernel pulls f_i from x - e_i in the
-// post-collision buffer A (ghost layers and the populations of solid cells that
-// face fluid have been filled beforehand, so the pull needs no boundary logic),
-// forms p = sum f / 3 and u = sum f e (the reference's LBM::Update,
-// "3D MPI+KOKKOS+MPIIO/lbm.cpp:384-415"), zeroes them in solid cells, applies the
-// reference profiles' inlet/outlet overrides, relaxes every population toward
-// feq_i = t_i (3p + 3 e.u + 4.5 (e.u)^2 - 1.5 u^2) with rate omega (the
-// reference's LBM::Collision, lbm.cpp:257-272, where omega = 1/(tau0+0.5)), and
-// writes the result to B.  This replaces the reference's five separate passes
-// (collision, stream1 into ft, stream2 copy-back, the host Update loop) by one
-// read and one write of every population.
+// For every interior cell X the kernels pull f_i(X) = f*_i(X - e_i) from the
+// post-collision buffer A, form p = sum f / 3 and u = sum f e (the reference's
+// LBM::Update, "3D MPI+KOKKOS+MPIIO/lbm.cpp:384-415"), zero them in solid cells,
+// relax every population toward feq_i = t_i (3p + 3 e.u + 4.5 (e.u)^2 - 1.5 u^2)
+// with rate omega = 1/(tau0 + 0.5) (the reference's LBM::Collision,
+// lbm.cpp:257-272) and write the next post-collision state to B.  This replaces
+// the reference's five passes (collision, stream1 into ft, stream2 copy-back,
+// the host Update loop, the boundary passes) by one read and one write of every
+// population.
 //
-// HBM traffic per cell update: Q loads + Q stores of the storage type (no reuse
-// is needed: in the SoA layout each population is a pure shift, so every
-// element of A is read exactly once per sweep) plus 1/8 byte of solid mask.
+// HBM traffic per cell update: Q loads + Q stores of the storage type (each
+// population is a pure shift, so every element of A is read exactly once) plus
+// 1/8 byte of solid mask.
+//
+// Three kernels:
+//   sweep_kernel          -- reference profiles: ghost layers and solid cells
+//                            were filled by the boundary passes, so the pull is
+//                            plain; applies the reference's inlet/outlet
+//                            overrides of Update.
+//   sweep_fast_kernel     -- channel profile, warp tiles away from the y/z faces
+//                            and from solids: plain pull, inlet/outlet by select.
+//   sweep_resolve_kernel  -- channel profile, the remaining warp tiles (listed):
+//                            resolves every source in the kernel and reduces the
+//                            momentum-exchange force on the body.
+// Splitting the channel sweep keeps the resolving code's registers out of the
+// kernel that does 95%+ of the cells.
 #pragma once
+#include <utility>
 #include "solver.cuh"
 
 namespace cflbm {
 
-template <int Q, class ST, class A, int MINB>
-__global__ void __launch_bounds__(128, MINB) sweep_kernel(const SweepArgs a) {
-  using L = Lat<Q>;
-  using SF = Store<ST>;
-  using E = typename SF::elem;
-  const int x = blockIdx.x * 32 + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  if (x >= a.L.nx || y >= a.L.ny) return;
-  const long long S = a.L.S;
-  const long long c = a.L.idx(x, y, z);
-  const long long row = a.L.px;
-  const long long plane = (long long)a.L.px * a.L.nyp;
-  const E *__restrict__ fa = static_cast<const E *>(a.fa);
-  E *__restrict__ fb = static_cast<E *>(a.fb);
-
-  A f[Q];
-#pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    const long long o = L::ex(i) + L::ey(i) * row + L::ez(i) * plane;
-    f[i] = SF::template load<A, L>(fa + i * S + c - o, i);
-  }
-
-  // Moments (deviation form: rho3 = 3p = sum f, u = sum f e).
-  A rho3 = f[0], ux = A(0), uy = A(0), uz = A(0);
-#pragma unroll
-  for (int k = 0; k < L::NPAIR; ++k) {
-    const int i = L::pair(k), j = L::opp(L::pair(k));
-    const A s = f[i] + f[j];
-    const A d = f[i] - f[j];
-    rho3 += s;
-    if (L::ex(i) > 0) ux += d; else if (L::ex(i) < 0) ux -= d;
-    if (L::ey(i) > 0) uy += d; else if (L::ey(i) < 0) uy -= d;
-    if (L::ez(i) > 0) uz += d; else if (L::ez(i) < 0) uz -= d;
-  }
-  const long long cell = ((long long)z * a.L.ny + y) * a.L.nx + x;
-  if (mask_solid(a.mask, a.nxw, a.L.ny, x, y, z)) {
-    rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
-  }
-  if (a.ref_override) {
-    if (x == 0) {
-      ux = static_cast<A>(a.inlet_u[(long long)z * a.L.ny + y]);
-      uy = A(0);
-      uz = A(0);
-    }
-    if (x == a.L.nx - 1) rho3 = A(0);
-  }
-  if (a.mu) {
-    a.mu[cell] = static_cast<double>(ux);
-    a.mv[cell] = static_cast<double>(uy);
-    a.mw[cell] = static_cast<double>(uz);
-    a.mp[cell] = static_cast<double>(rho3) / 3.0;
-  }
-  if (a.alpha) {
-    const A s = A(1) - static_cast<A>(a.alpha[cell]);
-    ux *= s;
-    uy *= s;
-    uz *= s;
-  }
-
-  // BGK relaxation, written per +/- pair: the pair shares (e.u)^2 and the
-  // even part of feq; the odd part flips sign.
+// BGK relaxation toward the incompressible equilibrium, written per +/- pair:
+// the pair shares (e.u)^2 and the even part of feq; the odd part flips sign.
+template <class L, class A>
+__device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const SweepArgs &a) {
   A om;
   if constexpr (sizeof(A) == 8) om = a.omega; else om = a.omega_f;
   const A c0 = rho3 - A(1.5) * (ux * ux + uy * uy + uz * uz);
@@ -98,17 +52,319 @@ __global__ void __launch_bounds__(128, MINB) sweep_kernel(const SweepArgs a) {
     f[i] = f[i] + om * ((sym + asym) - f[i]);
     f[j] = f[j] + om * ((sym - asym) - f[j]);
   }
+}
 
+// Moments in deviation form: rho3 = 3p = sum f, u = sum f e.
+template <class L, class A>
+__device__ __forceinline__ void moments(const A *f, A &rho3, A &ux, A &uy, A &uz) {
+  rho3 = f[0];
+  ux = A(0);
+  uy = A(0);
+  uz = A(0);
 #pragma unroll
-  for (int i = 0; i < Q; ++i) SF::template store<A, L>(fb + i * S + c, f[i], i);
+  for (int k = 0; k < L::NPAIR; ++k) {
+    const int i = L::pair(k), j = L::opp(L::pair(k));
+    const A s = f[i] + f[j];
+    const A d = f[i] - f[j];
+    rho3 += s;
+    if (L::ex(i) > 0) ux += d; else if (L::ex(i) < 0) ux -= d;
+    if (L::ey(i) > 0) uy += d; else if (L::ey(i) < 0) uy -= d;
+    if (L::ez(i) > 0) uz += d; else if (L::ez(i) < 0) uz -= d;
+  }
+}
+
+// Macros out (when requested), Brinkman damping of the equilibrium velocity,
+// relaxation, store: the common tail of every sweep.
+template <class L, class SF, class A, class E>
+__device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long long cell,
+                                            bool store, E *__restrict__ fb, long long c,
+                                            long long S, const SweepArgs &a) {
+  if (a.mu && store) {
+    a.mu[cell] = static_cast<double>(ux);
+    a.mv[cell] = static_cast<double>(uy);
+    a.mw[cell] = static_cast<double>(uz);
+    a.mp[cell] = static_cast<double>(rho3) / 3.0;
+  }
+  if (a.alpha) {
+    const A s = A(1) - static_cast<A>(a.alpha[cell]);
+    ux *= s;
+    uy *= s;
+    uz *= s;
+  }
+  bgk_relax<L, A>(f, rho3, ux, uy, uz, a);
+  if (store) {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) SF::template store<A, L>(fb + i * S + c, f[i], i);
+  }
+}
+
+// ---- reference profiles --------------------------------------------------------
+template <int Q, class ST, class A, int MINB>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_kernel(const SweepArgs a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int x = blockIdx.x * SWEEP_BX + threadIdx.x;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= a.L.nx || y >= a.L.ny) return;
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  E *__restrict__ fb = static_cast<E *>(a.fb);
+
+  A f[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i)
+    f[i] = SF::template load<A, L>(fa + i * S + c - a.L.off(L::ex(i), L::ey(i), L::ez(i)), i);
+
+  A rho3, ux, uy, uz;
+  moments<L, A>(f, rho3, ux, uy, uz);
+  const long long cell = ((long long)z * a.L.ny + y) * a.L.nx + x;
+  if (mask_solid(a.mask, a.nxw, a.L.ny, x, y, z)) {
+    rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
+  }
+  if (a.ref_override) {
+    if (x == 0) {
+      ux = static_cast<A>(a.inlet_u[(long long)z * a.L.ny + y]);
+      uy = A(0);
+      uz = A(0);
+    }
+    if (x == a.L.nx - 1) rho3 = A(0);
+  }
+  finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, true, fb, c, S, a);
 }
 
 template <int Q, class ST, class A, int MINB>
 cudaError_t launch_sweep_t(const SweepArgs &a, cudaStream_t s) {
-  dim3 block(32, 4, 1);
-  dim3 grid((a.L.nx + 31) / 32, (a.L.ny + 3) / 4, a.L.nz);
+  dim3 block(SWEEP_BX, SWEEP_BY, 1);
+  dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
   sweep_kernel<Q, ST, A, MINB><<<grid, block, 0, s>>>(a);
   count_launch();
+  return cudaGetLastError();
+}
+
+// ---- channel profile -------------------------------------------------------------
+// Compile-time data of direction I: velocity, opposite and the specular
+// mirrors in y, z and both.
+template <int Q, int I> struct DirC {
+  using L = Lat<Q>;
+  static constexpr int ex = L::ex(I), ey = L::ey(I), ez = L::ez(I), opp = L::opp(I);
+  static constexpr int my = mirror<L>(I, 1), mz = mirror<L>(I, 2);
+  static constexpr int myz = mirror<L>(mirror<L>(I, 1), 2);
+};
+
+template <class F, int... Is>
+__device__ __forceinline__ void static_for(F &&f, std::integer_sequence<int, Is...>) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+
+// Interior warp tiles: no y/z face and no solid within one lattice step, so the
+// pull is plain; the inlet column takes the inlet equilibrium and the outlet
+// column repeats itself (zero gradient) through selects.
+template <int Q, class ST, class A, int MINB>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_fast_kernel(const SweepArgs a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y;
+  const int z = blockIdx.z;
+  if (y >= a.L.ny) return;
+  if (a.tile_slow[((long long)z * a.L.ny + y) * a.nxw + blockIdx.x]) return;  // warp-uniform
+  const int xr = blockIdx.x * SWEEP_BX + threadIdx.x;
+  const bool valid = xr < nx;
+  const int x = valid ? xr : nx - 1;
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  E *__restrict__ fb = static_cast<E *>(a.fb);
+  A f[Q];
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        using Dd = DirC<Q, I>;
+        const long long o = a.L.off(Dd::ex, Dd::ey, Dd::ez);
+        if constexpr (Dd::ex > 0) {
+          f[I] = (x == 0) ? static_cast<A>(a.f_in[I])
+                          : SF::template load<A, L>(fa + I * S + c - o, I);
+        } else if constexpr (Dd::ex < 0) {
+          const long long adj = (x == nx - 1) ? Dd::ex : 0;  // zero-gradient outlet
+          f[I] = SF::template load<A, L>(fa + I * S + c - o + adj, I);
+        } else {
+          f[I] = SF::template load<A, L>(fa + I * S + c - o, I);
+        }
+      },
+      std::make_integer_sequence<int, Q>{});
+  A rho3, ux, uy, uz;
+  moments<L, A>(f, rho3, ux, uy, uz);
+  const long long cell = ((long long)z * a.L.ny + y) * nx + x;
+  finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
+}
+
+// Listed warp tiles: every source X - e_i is resolved --
+//   z outside [0,nz): periodic wrap / free-slip mirror (i -> mirror_z(i), source
+//   z := X.z) / no-slip halfway bounce-back (f*_{opp(i)}(X)); then the same in y;
+//   x < 0: inlet equilibrium; x >= nx: zero gradient (x := nx-1); solid source:
+//   halfway bounce-back f*_{opp(i)}(X).
+// Each solid bounce-back at a fluid cell adds its momentum exchange
+// 2 f*_{opp(i)}(X) e_{opp(i)} to the body force (FP64), reduced by warp
+// shuffles, per block, and over blocks by the last block in block order, into
+// the force-history slot of this step.
+template <int Q, class ST, class A, int MINB>
+__global__ void __launch_bounds__(32 * SLOW_TILES_PER_BLOCK, MINB)
+    sweep_resolve_kernel(const SweepArgs a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx, ny = a.L.ny, nz = a.L.nz;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long long t = (long long)blockIdx.x * SLOW_TILES_PER_BLOCK + wid;
+  double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+  if (t < a.n_slow) {  // warp-uniform
+    const int tile = a.slow_tiles[t];
+    const int xw = tile % a.nxw;
+    const int row = tile / a.nxw;
+    const int y = row % ny, z = row / ny;
+    const int xr = xw * 32 + lane;
+    const bool valid = xr < nx;
+    const int x = valid ? xr : nx - 1;
+    const long long S = a.L.S;
+    const long long c = a.L.idx(x, y, z);
+    const E *__restrict__ fa = static_cast<const E *>(a.fa);
+    E *__restrict__ fb = static_cast<E *>(a.fb);
+    const bool solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
+    A f[Q];
+    static_for(
+        [&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          using Dd = DirC<Q, I>;
+          if constexpr (I == 0) {
+            f[0] = SF::template load<A, L>(fa + c, 0);
+          } else {
+            int sx = x - Dd::ex, sy = y - Dd::ey, sz = z - Dd::ez;
+            bool my = false, mz = false, bb = false, hit = false;
+            if constexpr (Dd::ez != 0) {
+              if (sz < 0 || sz >= nz) {
+                if (a.wall_z == WALL_PERIODIC) sz = sz < 0 ? sz + nz : sz - nz;
+                else if (a.wall_z == WALL_FREESLIP) { mz = true; sz = z; }
+                else bb = true;
+              }
+            }
+            if constexpr (Dd::ey != 0) {
+              if (!bb && (sy < 0 || sy >= ny)) {
+                if (a.wall_y == WALL_PERIODIC) sy = sy < 0 ? sy + ny : sy - ny;
+                else if (a.wall_y == WALL_FREESLIP) { my = true; sy = y; }
+                else bb = true;
+              }
+            }
+            A v = A(0);
+            if (!bb) {
+              const int j = my ? (mz ? Dd::myz : Dd::my) : (mz ? Dd::mz : I);
+              if (Dd::ex > 0 && sx < 0) {
+                v = static_cast<A>(a.f_in[j]);
+              } else {
+                if (sx >= nx) sx = nx - 1;
+                if (mask_solid(a.mask, a.nxw, ny, sx, sy, sz)) {
+                  bb = true;
+                  hit = true;
+                } else {
+                  // mirrors keep |e|, so direction I's storage scale applies to j
+                  v = SF::template load<A, L>(fa + j * S + a.L.idx(sx, sy, sz), I);
+                }
+              }
+            }
+            if (bb) {
+              v = SF::template load<A, L>(fa + Dd::opp * S + c, Dd::opp);
+              if (hit && valid && !solid_here) {
+                const double m = 2.0 * static_cast<double>(v);
+                Fx -= m * Dd::ex;
+                Fy -= m * Dd::ey;
+                Fz -= m * Dd::ez;
+              }
+            }
+            f[I] = v;
+          }
+        },
+        std::make_integer_sequence<int, Q>{});
+    A rho3, ux, uy, uz;
+    moments<L, A>(f, rho3, ux, uy, uz);
+    if (solid_here) {
+      rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
+    }
+    const long long cell = ((long long)z * ny + y) * nx + x;
+    finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
+  }
+
+  // Block partial -> partials[blockIdx.x]; the last block sums all partials.
+  constexpr int NW = SLOW_TILES_PER_BLOCK;
+  __shared__ double sh[3][NW];
+  __shared__ bool last;
+  for (int o = 16; o > 0; o >>= 1) {
+    Fx += __shfl_down_sync(0xffffffffu, Fx, o);
+    Fy += __shfl_down_sync(0xffffffffu, Fy, o);
+    Fz += __shfl_down_sync(0xffffffffu, Fz, o);
+  }
+  if (lane == 0) {
+    sh[0][wid] = Fx;
+    sh[1][wid] = Fy;
+    sh[2][wid] = Fz;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bx = 0.0, by = 0.0, bz = 0.0;
+    for (int w = 0; w < NW; ++w) { bx += sh[0][w]; by += sh[1][w]; bz += sh[2][w]; }
+    a.partials[3 * blockIdx.x] = bx;
+    a.partials[3 * blockIdx.x + 1] = by;
+    a.partials[3 * blockIdx.x + 2] = bz;
+    __threadfence();
+    last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    const volatile double *p = a.partials;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+      s0 += p[3 * k];
+      s1 += p[3 * k + 1];
+      s2 += p[3 * k + 2];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+      s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+      sh[0][wid] = s0;
+      sh[1][wid] = s1;
+      sh[2][wid] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tx = 0.0, ty = 0.0, tz = 0.0;
+      for (int w = 0; w < NW; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
+      const long long st = *a.step;
+      double *h = a.hist + 3 * (st % a.cap);
+      h[0] = tx;
+      h[1] = ty;
+      h[2] = tz;
+      *a.step = st + 1;
+      *a.counter = 0u;
+    }
+  }
+}
+
+template <int Q, class ST, class A, int MINB_FAST, int MINB_SLOW>
+cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s) {
+  dim3 block(SWEEP_BX, SWEEP_BY, 1);
+  dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
+  sweep_fast_kernel<Q, ST, A, MINB_FAST><<<grid, block, 0, s>>>(a);
+  const int sb = (a.n_slow + SLOW_TILES_PER_BLOCK - 1) / SLOW_TILES_PER_BLOCK;
+  sweep_resolve_kernel<Q, ST, A, MINB_SLOW>
+      <<<sb > 0 ? sb : 1, 32 * SLOW_TILES_PER_BLOCK, 0, s>>>(a);
+  count_launch(2);
   return cudaGetLastError();
 }
 

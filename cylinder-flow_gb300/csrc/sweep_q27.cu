@@ -20,4 +20,22 @@ cudaError_t launch_sweep_q27(int store, int compute, const SweepArgs &a, cudaStr
   return cudaErrorInvalidValue;
 }
 
+cudaError_t launch_sweep_channel_q27(int store, int compute, const SweepArgs &a,
+                                     cudaStream_t s) {
+  if (compute == COMPUTE_F64) {
+    switch (store) {
+      case STORE_F64: return launch_sweep_channel_t<27, double, double, 3, 2>(a, s);
+      case STORE_F32: return launch_sweep_channel_t<27, float, double, 3, 2>(a, s);
+      case STORE_F16: return launch_sweep_channel_t<27, F16Dev, double, 3, 2>(a, s);
+    }
+  } else {
+    switch (store) {
+      case STORE_F64: return launch_sweep_channel_t<27, double, float, 8, 2>(a, s);
+      case STORE_F32: return launch_sweep_channel_t<27, float, float, 8, 2>(a, s);
+      case STORE_F16: return launch_sweep_channel_t<27, F16Dev, float, 8, 2>(a, s);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace cflbm

@@ -52,6 +52,10 @@ enum cflbm_compute { CFLBM_COMPUTE_FP64 = 0, CFLBM_COMPUTE_FP32 = 1 };
 enum cflbm_profile { CFLBM_PROFILE_CHANNEL = 0, CFLBM_PROFILE_REF2D = 1, CFLBM_PROFILE_REF3D = 2 };
 enum cflbm_wall { CFLBM_WALL_FREESLIP = 0, CFLBM_WALL_NOSLIP = 1, CFLBM_WALL_PERIODIC = 2 };
 enum cflbm_geom { CFLBM_GEOM_NONE = 0, CFLBM_GEOM_CYLINDER = 1, CFLBM_GEOM_SPHERE = 2 };
+/* Population layout in device memory (x fastest in both):
+ *  SOA:  f[i][z][y][x] -- one array per population;
+ *  ROWS: f[z][y][i][x] -- the Q rows of a (y, z) line are adjacent. */
+enum cflbm_layout { CFLBM_LAYOUT_SOA = 0, CFLBM_LAYOUT_ROWS = 1 };
 
 typedef struct cflbm_handle cflbm_handle;
 
@@ -76,6 +80,7 @@ typedef struct cflbm_config {
                              (its layout, (i*ly+j)*lz+k), or NULL for a seeded draw */
   int force_history;    /* capacity (steps) of the on-device force history; 0 = 65536 */
   int device;           /* CUDA device ordinal */
+  int layout;           /* enum cflbm_layout */
 } cflbm_config;
 
 /* Geometry/step counters and device layout of a handle. */
@@ -90,6 +95,7 @@ typedef struct cflbm_info {
   double omega;         /* 1/(tau0+0.5) */
   double bytes_per_cell_step; /* algorithmic HBM bytes per cell update of the sweep */
   size_t device_bytes;  /* device memory held by the handle */
+  int layout;           /* enum cflbm_layout */
 } cflbm_info;
 
 /* Defaults: D2Q9 64x32, FP64 storage and arithmetic, CHANNEL, free-slip y,

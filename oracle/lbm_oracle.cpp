@@ -574,7 +574,7 @@ int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out
       }
     }
   };
-  auto resolve = [&](int i0, int x, int y, int z) -> double {
+  auto resolve = [&](int i0, int x, int y, int z, bool *hit) -> double {
     int i = i0;
     int sx = x - e[i][0], sy = y - e[i][1], sz = z - e[i][2];
     if (Q == 27 && (sz < 0 || sz >= nz)) {
@@ -589,13 +589,18 @@ int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out
     }
     if (sx < 0) return f_in[i];
     if (sx >= nx) sx = nx - 1;
-    if (solid[cell(sx, sy, sz)]) return f[bb[i0] * N + cell(x, y, z)];
+    if (solid[cell(sx, sy, sz)]) {
+      if (hit) *hit = true;
+      return f[bb[i0] * N + cell(x, y, z)];
+    }
     return f[i * N + cell(sx, sy, sz)];
   };
 
   for (int it = 1; it <= steps; ++it) {
     collision();
-    // Momentum exchange on fluid->solid links (post-collision state).
+    // Momentum exchange on fluid->solid links (post-collision state): every
+    // pull of a fluid cell that bounces back off a solid source (after the
+    // periodic/mirror mapping) carries 2 f*_{bb(i)}(X) e_{bb(i)} into the body.
     double Fx = 0.0, Fy = 0.0, Fz = 0.0;
     for (int z = 0; z < nz; ++z)
       for (int y = 0; y < ny; ++y)
@@ -603,13 +608,13 @@ int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out
           long n = cell(x, y, z);
           if (solid[n]) continue;
           for (int ii = 1; ii < Q; ++ii) {
-            int X = x + e[ii][0], Y = y + e[ii][1], Z = z + e[ii][2];
-            if (X < 0 || X >= nx || Y < 0 || Y >= ny || Z < 0 || Z >= nz) continue;
-            if (!solid[cell(X, Y, Z)]) continue;
-            double mom = 2.0 * f[ii * N + n];
-            Fx += mom * e[ii][0];
-            Fy += mom * e[ii][1];
-            Fz += mom * e[ii][2];
+            bool hit = false;
+            double v = resolve(ii, x, y, z, &hit);
+            if (!hit) continue;
+            double mom = 2.0 * v;
+            Fx -= mom * e[ii][0];
+            Fy -= mom * e[ii][1];
+            Fz -= mom * e[ii][2];
           }
         }
     if (force_out) {
@@ -623,7 +628,7 @@ int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out
         for (int x = 0; x < nx; ++x) {
           long n = cell(x, y, z);
           for (int ii = 0; ii < Q; ++ii)
-            ft[ii * N + n] = (ii == 0) ? f[n] : resolve(ii, x, y, z);
+            ft[ii * N + n] = (ii == 0) ? f[n] : resolve(ii, x, y, z, nullptr);
         }
     std::swap(f, ft);
     // Update (reference form: p = sum f / 3, u = sum f e, zero in solids).

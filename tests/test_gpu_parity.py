@@ -180,6 +180,30 @@ def test_steps_are_deterministic_and_resumable(cuda):
         assert a.info().steps_done == b.info().steps_done == 17
 
 
+@pytest.mark.parametrize("name", ["d2q9_cyl_freeslip", "d3q27_cyl", "d3q27_noslip"])
+@pytest.mark.parametrize("storage", ["fp64", "fp16dev"])
+def test_layouts_give_identical_states(cuda, name, storage):
+    case = CHANNEL_CASES[name]
+    steps = 60 if case["lattice"] == 9 else 12
+    out = []
+    for layout in ("soa", "rows"):
+        with Solver(perturb_amp=1e-3, layout=layout, storage=storage, compute="fp32",
+                    **case) as s:
+            s.step(steps)
+            out.append((s.get_f(), s.force_history()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_reference_profile_rows_layout_matches_golden(cuda):
+    g = load_golden("ref3d_40x12x12")
+    m = g["meta"]
+    r = ref3d_gpu(m["nx"], m["ny"], m["nz"], m["tau0"], m["u0"], g["ran"], m["steps"],
+                  layout="rows")
+    for k in ("u", "v", "w", "p", "fpost"):
+        assert rel_err(r[k], g[k]) < TOL64, k
+
+
 def test_mass_and_momentum_sums(cuda):
     case = CHANNEL_CASES["d2q9_cyl_freeslip"]
     o = oracle_channel(case, 50)
@@ -226,4 +250,4 @@ def test_launches_are_counted(cuda):
     with Solver(**CHANNEL_CASES["d2q9_periodic"]) as s:
         s.step(5)
         s.synchronize()
-    assert cflbm.launch_count() - n0 >= 3 * 5
+    assert cflbm.launch_count() - n0 >= 2 * 5  # fast + resolving sweep per step
