@@ -13,6 +13,9 @@ using namespace cflbm;
 
 namespace {
 
+// Steps per captured CUDA graph (even: A/B parity is preserved by a replay).
+constexpr int GRAPH_STEPS = 64;
+
 thread_local std::string g_last_error;
 
 int fail(int code, const char *fmt, ...) {
@@ -63,6 +66,8 @@ void free_handle(cflbm_handle *h) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  for (cudaGraphExec_t g : h->graph_exec)
+    if (g) cudaGraphExecDestroy(g);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -304,6 +309,8 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   h->f_bytes = (size_t)L.total * es;
   if ((rc = dev_alloc(h, &h->fA, h->f_bytes))) return rc;
   if ((rc = dev_alloc(h, &h->fB, h->f_bytes))) return rc;
+  h->buf[0] = h->fA;
+  h->buf[1] = h->fB;
   CK_CUDA(cudaMemsetAsync(h->fA, 0, h->f_bytes, h->stream));
   CK_CUDA(cudaMemsetAsync(h->fB, 0, h->f_bytes, h->stream));
   if ((rc = dev_alloc_t(h, &h->d_mask, mask.size()))) return rc;
@@ -469,7 +476,10 @@ static int one_step(cflbm_handle *h, bool write_macros) {
     sa.near = h->d_near;
     sa.wall_y = h->cfg.wall_y;
     sa.wall_z = h->cfg.wall_z;
-    for (int i = 0; i < Q; ++i) sa.f_in[i] = h->f_in[i];
+    for (int i = 0; i < Q; ++i) {
+      sa.f_in[i] = h->f_in[i];
+      sa.f_in_f[i] = (float)h->f_in[i];
+    }
     sa.tile_slow = h->d_tile_slow;
     sa.slow_tiles = h->d_slow_tiles;
     sa.n_slow = h->n_slow;
@@ -546,8 +556,40 @@ int cflbm_step(cflbm_handle *h, int nsteps) {
   if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
   if (nsteps < 0) return fail(CFLBM_E_INVALID, "nsteps < 0");
   CK_CUDA(cudaSetDevice(h->cfg.device));
-  for (int s = 0; s < nsteps; ++s) {
-    int rc = one_step(h, s == nsteps - 1);
+  int left = nsteps;
+  // Long calls replay a captured CUDA graph of GRAPH_STEPS steps (an even count,
+  // so the A/B parity is unchanged), one graph per parity, captured on first use.
+  // The last step always runs directly so it can write the macroscopic fields.
+  while (!h->timing && left > GRAPH_STEPS) {
+    const int par = h->fA == h->buf[0] ? 0 : 1;
+    if (!h->graph_exec[par]) {
+      cudaGraph_t g = nullptr;
+      const long long n0 = launches();
+      CK_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = CFLBM_OK;
+      for (int s = 0; s < GRAPH_STEPS && rc == CFLBM_OK; ++s) rc = one_step(h, false);
+      cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      CK_CUDA(ec);
+      cudaError_t ei = cudaGraphInstantiate(&h->graph_exec[par], g, 0);
+      cudaGraphDestroy(g);
+      CK_CUDA(ei);
+      h->launches_per_step = (launches() - n0) / GRAPH_STEPS;
+      // Capture advanced the host-side step state (and counted the captured
+      // launches) without running anything; this first replay runs them.
+      CK_CUDA(cudaGraphLaunch(h->graph_exec[par], h->stream));
+    } else {
+      CK_CUDA(cudaGraphLaunch(h->graph_exec[par], h->stream));
+      h->steps_done += GRAPH_STEPS;
+      count_launch((long long)GRAPH_STEPS * h->launches_per_step);
+    }
+    left -= GRAPH_STEPS;
+  }
+  for (int s = 0; s < left; ++s) {
+    int rc = one_step(h, s == left - 1);
     if (rc) return rc;
   }
   return CFLBM_OK;

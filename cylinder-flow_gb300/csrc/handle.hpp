@@ -43,6 +43,10 @@ struct cflbm_handle {
   double area = 1.0;  // Cd/Cl reference area
   size_t device_bytes = 0;
   // Kernel timing (cflbm_set_timing): event pairs around sweeps / boundary phases.
+  // CUDA graphs of GRAPH_STEPS steps, one per A/B parity (buf[0] = A at create).
+  void *buf[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  long long launches_per_step = 0;
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;

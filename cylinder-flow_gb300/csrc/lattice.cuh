@@ -97,12 +97,46 @@ template <class T> struct Store;
 
 #if defined(__CUDACC__)
 
+// double <-> float on the integer pipe.  On GB300 the F2F conversions run on
+// the FP64 units (~0.5 T/s), which would cap an FP64-storage / FP32-arithmetic
+// sweep at ~9 G cell updates/s; these take ~7 integer operations each.
+//   f2d: exact for normal floats and zero; subnormal floats flush to zero;
+//        infinities and NaNs are kept.
+//   d2f: rounds the 29 dropped mantissa bits half up; |d| < 2^-126 flushes to
+//        zero; |d| >= 2^128, infinities and NaNs become infinity.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned ex = u & 0x7F800000u;
+  unsigned hi = (((u >> 3) & 0x0FFFFFFFu) + (896u << 20)) | sign;
+  unsigned lo = u << 29;
+  if (ex == 0u) { hi = sign; lo = 0u; }
+  if (ex == 0x7F800000u) hi |= 0x7FF00000u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ float d2f_bits(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d);
+  const unsigned lo = (unsigned)__double2loint(d);
+  const unsigned mag = hi & 0x7FFFFFFFu;
+  unsigned t = __funnelshift_l(lo, hi, 3);  // exponent (low 9 bits) and 23 mantissa bits
+  t = ((t - 0xC0000000u) & 0x7FFFFFFFu) + ((lo >> 28) & 1u);  // (896 << 23) mod 2^32
+  if (mag < (897u << 20)) t = 0u;
+  if (mag >= (1151u << 20)) t = 0x7F800000u;
+  return __uint_as_float(t | (hi & 0x80000000u));
+}
+
 template <> struct Store<double> {
   using elem = double;
   template <class A, class L>
-  __device__ static A load(const elem *p, int) { return static_cast<A>(__ldg(p)); }
+  __device__ static A load(const elem *p, int) {
+    if constexpr (sizeof(A) == 4) return d2f_bits(__ldg(p));
+    else return static_cast<A>(__ldg(p));
+  }
   template <class A, class L>
-  __device__ static void store(elem *p, A v, int) { *p = static_cast<double>(v); }
+  __device__ static void store(elem *p, A v, int) {
+    if constexpr (sizeof(A) == 4) *p = f2d_bits(v);
+    else *p = static_cast<double>(v);
+  }
 };
 
 template <> struct Store<float> {

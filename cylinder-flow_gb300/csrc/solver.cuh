@@ -66,6 +66,7 @@ struct SweepArgs {
   const uint32_t *near;  // bit-packed: cell is solid or has a solid neighbour
   int wall_y, wall_z;
   double f_in[27];       // inlet equilibrium populations (p = 0, u = (u_in, 0, 0))
+  float f_in_f[27];      // the same in FP32 (FP32-arithmetic sweeps)
   const unsigned char *tile_slow;  // per warp tile (32 cells of a row): 1 = resolve
   const int *slow_tiles; // list of resolving tiles (tile = (z*ny + y)*nxw + x/32)
   int n_slow;            // length of the list

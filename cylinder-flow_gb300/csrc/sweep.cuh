@@ -80,10 +80,17 @@ __device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long
                                             bool store, E *__restrict__ fb, long long c,
                                             long long S, const SweepArgs &a) {
   if (a.mu && store) {
-    a.mu[cell] = static_cast<double>(ux);
-    a.mv[cell] = static_cast<double>(uy);
-    a.mw[cell] = static_cast<double>(uz);
-    a.mp[cell] = static_cast<double>(rho3) / 3.0;
+    if constexpr (sizeof(A) == 4) {
+      a.mu[cell] = f2d_bits(ux);
+      a.mv[cell] = f2d_bits(uy);
+      a.mw[cell] = f2d_bits(uz);
+      a.mp[cell] = f2d_bits(rho3 * (1.0f / 3.0f));
+    } else {
+      a.mu[cell] = ux;
+      a.mv[cell] = uy;
+      a.mw[cell] = uz;
+      a.mp[cell] = rho3 / 3.0;
+    }
   }
   if (a.alpha) {
     const A s = A(1) - static_cast<A>(a.alpha[cell]);
@@ -159,6 +166,13 @@ __device__ __forceinline__ void static_for(F &&f, std::integer_sequence<int, Is.
   (f(std::integral_constant<int, Is>{}), ...);
 }
 
+// Inlet equilibrium population in the arithmetic type (no FP64 conversion in
+// FP32 sweeps).
+template <class A>
+__device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
+  if constexpr (sizeof(A) == 8) return a.f_in[i]; else return a.f_in_f[i];
+}
+
 // Interior warp tiles: no y/z face and no solid within one lattice step, so the
 // pull is plain; the inlet column takes the inlet equilibrium and the outlet
 // column repeats itself (zero gradient) through selects.
@@ -186,8 +200,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_fast_kernel(c
         using Dd = DirC<Q, I>;
         const long long o = a.L.off(Dd::ex, Dd::ey, Dd::ez);
         if constexpr (Dd::ex > 0) {
-          f[I] = (x == 0) ? static_cast<A>(a.f_in[I])
-                          : SF::template load<A, L>(fa + I * S + c - o, I);
+          f[I] = (x == 0) ? inlet_pop<A>(a, I) : SF::template load<A, L>(fa + I * S + c - o, I);
         } else if constexpr (Dd::ex < 0) {
           const long long adj = (x == nx - 1) ? Dd::ex : 0;  // zero-gradient outlet
           f[I] = SF::template load<A, L>(fa + I * S + c - o + adj, I);
@@ -262,7 +275,7 @@ __global__ void __launch_bounds__(32 * SLOW_TILES_PER_BLOCK, MINB)
             if (!bb) {
               const int j = my ? (mz ? Dd::myz : Dd::my) : (mz ? Dd::mz : I);
               if (Dd::ex > 0 && sx < 0) {
-                v = static_cast<A>(a.f_in[j]);
+                v = inlet_pop<A>(a, j);
               } else {
                 if (sx >= nx) sx = nx - 1;
                 if (mask_solid(a.mask, a.nxw, ny, sx, sy, sz)) {
