@@ -76,6 +76,9 @@ SIGNATURES = {
     "cflbm_get_stream": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "cflbm_set_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "cflbm_get_timing": ([ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cflbm_domain_sums_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "cflbm_last_error": ([], ctypes.c_char_p),
     "cflbm_launch_count": ([], ctypes.c_int64),
 }

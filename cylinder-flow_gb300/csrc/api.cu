@@ -811,3 +811,8 @@ int cflbm_write_tecplot_fields(const char *path, int dim, int nx, int ny, int nz
 }
 
 }  // extern "C"
+
+namespace cflbm {
+// Error reporting for entry points defined in other translation units.
+int record_error(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace cflbm

@@ -183,6 +183,31 @@ int cflbm_get_stream(cflbm_handle *h, void **stream);
 int cflbm_set_timing(cflbm_handle *h, int enable);
 int cflbm_get_timing(cflbm_handle *h, double ms[2], int64_t counts[2]);
 
+/* Domain sums that allocate nothing -- no counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc (a memory pool or framework that owns
+ * every device byte, a fixed memory budget, code running where allocation is
+ * forbidden) but hold populations in device memory.  cflbm_mass() needs a
+ * handle, and creating one allocates; this call needs none.
+ *
+ * d_f:     device array, dense [i][z][y][x] (x fastest), q*nx*ny*nz elements of
+ *          the storage type (FP16DEV: f_i times the lattice's per-direction
+ *          power-of-two scale, as cflbm stores it).
+ * d_solid: optional device uint8 mask, nx*ny*nz (1 = solid, skipped), or NULL.
+ * d_out:   device, 4 doubles: sum over fluid cells of (1 + sum_i f_i), then the
+ *          momentum sum_i f_i e_i (x, y, z); all accumulated in FP64.
+ * stream:  cudaStream_t to launch on (NULL = legacy default stream).
+ *
+ * Scratch (per-block partials and a completion counter) is a file-scope device
+ * array of 512 KiB held by every GPU that loads the library until exit; grids of
+ * more than 134,217,728 cells are rejected with CFLBM_E_INVALID.  The first call
+ * on a device looks up the array's device address; make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race.
+ * Asynchronous: read d_out after synchronising the stream. */
+int cflbm_domain_sums_noalloc(int lattice, int storage, int nx, int ny, int nz,
+                              const void *d_f, const uint8_t *d_solid, double *d_out,
+                              void *stream);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char *cflbm_last_error(void);
 
