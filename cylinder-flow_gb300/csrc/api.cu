@@ -60,7 +60,7 @@ void free_handle(cflbm_handle *h) {
   if (h->cfg.device >= 0) cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
-                  h->d_near, h->d_tile_slow, h->d_slow_tiles,
+                  h->d_links_bits, h->d_tile_slow, h->d_slow_tiles,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
                   h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
   for (void *p : ptrs)
@@ -108,42 +108,66 @@ void build_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
       }
 }
 
-// Cells that are solid or have a solid neighbour (any lattice direction).
+// Channel-profile solid links: bit i of cell X is set when the source of
+// population i, X - e_i mapped onto the box exactly as the sweep maps it
+// (periodic wrap / free-slip mirror / no-slip wall / inlet / zero-gradient
+// outlet), is a solid cell -- i.e. when the sweep must bounce population i back.
 template <int Q>
-std::vector<uint8_t> near_solid(const std::vector<uint8_t> &solid, int nx, int ny, int nz) {
+std::vector<uint32_t> channel_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
+                                    int wall_y, int wall_z) {
   using L = Lat<Q>;
-  std::vector<uint8_t> nr(solid.size(), 0);
+  std::vector<uint32_t> bits(solid.size(), 0u);
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
-        const size_t n = ((size_t)z * ny + y) * nx + x;
-        if (solid[n]) { nr[n] = 1; continue; }
-        for (int k = 1; k < Q; ++k) {
-          const int X = x + L::ex(k), Y = y + L::ey(k), Z = z + L::ez(k);
-          if (X < 0 || X >= nx || Y < 0 || Y >= ny || Z < 0 || Z >= nz) continue;
-          if (solid[((size_t)Z * ny + Y) * nx + X]) { nr[n] = 1; break; }
+        uint32_t b = 0u;
+        for (int i = 1; i < Q; ++i) {
+          int sx = x - L::ex(i), sy = y - L::ey(i), sz = z - L::ez(i);
+          if (Q == 27 && (sz < 0 || sz >= nz)) {
+            if (wall_z == CFLBM_WALL_PERIODIC) sz = (sz + nz) % nz;
+            else if (wall_z == CFLBM_WALL_FREESLIP) sz = z;
+            else continue;  // no-slip wall, not the body
+          }
+          if (sy < 0 || sy >= ny) {
+            if (wall_y == CFLBM_WALL_PERIODIC) sy = (sy + ny) % ny;
+            else if (wall_y == CFLBM_WALL_FREESLIP) sy = y;
+            else continue;
+          }
+          if (sx < 0) continue;  // inlet
+          if (sx >= nx) sx = nx - 1;
+          if (solid[((size_t)sz * ny + sy) * nx + sx]) b |= 1u << i;
         }
+        bits[((size_t)z * ny + y) * nx + x] = b;
       }
-  return nr;
+  return bits;
 }
 
-// Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) that the
-// channel sweep must resolve: on a y or z face, or holding a cell that is solid
-// or next to a solid.  Returns the per-tile flags and fills the list.
-std::vector<unsigned char> slow_tiles(const std::vector<uint8_t> &nr, int nx, int ny, int nz,
-                                      int nxw, bool d3, std::vector<int> &list) {
+// Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) holding a
+// solid cell or a cell with solid links: the second channel launch handles
+// them.  Fills the list and the 32 link words of every listed tile; returns the
+// per-tile flags.
+std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
+                                       const std::vector<uint32_t> &bits, int nx, int ny,
+                                       int nz, int nxw, std::vector<int> &list,
+                                       std::vector<uint32_t> &tile_bits) {
   std::vector<unsigned char> flag((size_t)nxw * ny * nz, 0);
   list.clear();
+  tile_bits.clear();
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int w = 0; w < nxw; ++w) {
-        bool slow = y == 0 || y == ny - 1 || (d3 && (z == 0 || z == nz - 1));
-        for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !slow; ++x)
-          if (nr[((size_t)z * ny + y) * nx + x]) slow = true;
-        if (slow) {
-          const size_t t = ((size_t)z * ny + y) * nxw + w;
-          flag[t] = 1;
-          list.push_back((int)t);
+        bool any = false;
+        for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !any; ++x) {
+          const size_t n = ((size_t)z * ny + y) * nx + x;
+          any = solid[n] || bits[n];
+        }
+        if (!any) continue;
+        const size_t t = ((size_t)z * ny + y) * nxw + w;
+        flag[t] = 1;
+        list.push_back((int)t);
+        for (int l = 0; l < 32; ++l) {
+          const int x = w * 32 + l;
+          tile_bits.push_back(x < nx ? bits[((size_t)z * ny + y) * nx + x] : 0u);
         }
       }
   return flag;
@@ -331,22 +355,25 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   h->link_blocks = (int)std::min<long long>(std::max<long long>((h->n_links + 255) / 256, 1), 1024);
   h->reduce_blocks = (int)std::min<long long>(std::max<long long>(((long long)N + 255) / 256, 1), 2048);
   if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
-    const std::vector<uint8_t> nr = d3 ? near_solid<27>(solid, nx, ny, nz)
-                                       : near_solid<9>(solid, nx, ny, nz);
-    const std::vector<uint32_t> nearw = pack_mask(nr, nx, ny, nz, h->nxw);
-    if ((rc = dev_alloc_t(h, &h->d_near, nearw.size()))) return rc;
-    CK_CUDA(cudaMemcpyAsync(h->d_near, nearw.data(), nearw.size() * 4, cudaMemcpyHostToDevice,
-                            h->stream));
+    const std::vector<uint32_t> bits =
+        d3 ? channel_links<27>(solid, nx, ny, nz, cfg->wall_y, cfg->wall_z)
+           : channel_links<9>(solid, nx, ny, nz, cfg->wall_y, cfg->wall_z);
     std::vector<int> list;
-    const std::vector<unsigned char> flag = slow_tiles(nr, nx, ny, nz, h->nxw, d3, list);
+    std::vector<uint32_t> tile_bits;
+    const std::vector<unsigned char> flag =
+        solid_tiles(solid, bits, nx, ny, nz, h->nxw, list, tile_bits);
     h->n_slow = (int)list.size();
     if ((rc = dev_alloc_t(h, &h->d_tile_slow, flag.size()))) return rc;
     CK_CUDA(cudaMemcpyAsync(h->d_tile_slow, flag.data(), flag.size(), cudaMemcpyHostToDevice,
                             h->stream));
     if ((rc = dev_alloc_t(h, &h->d_slow_tiles, list.size() + 1))) return rc;
-    if (!list.empty())
+    if ((rc = dev_alloc_t(h, &h->d_links_bits, tile_bits.size() + 32))) return rc;
+    if (!list.empty()) {
       CK_CUDA(cudaMemcpyAsync(h->d_slow_tiles, list.data(), list.size() * sizeof(int),
                               cudaMemcpyHostToDevice, h->stream));
+      CK_CUDA(cudaMemcpyAsync(h->d_links_bits, tile_bits.data(), tile_bits.size() * 4,
+                              cudaMemcpyHostToDevice, h->stream));
+    }
     CK_CUDA(cudaStreamSynchronize(h->stream));
     for (int i = 0; i < Q; ++i) {
       const int ex = d3 ? Lat<27>::ex(i) : Lat<9>::ex(i);
@@ -357,7 +384,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     CK_CUDA(cudaStreamSynchronize(h->stream));  // host vectors die at scope end
   }
   const size_t nparts = std::max<size_t>(4 * (size_t)std::max(h->link_blocks, h->reduce_blocks),
-                                         3 * (size_t)std::max((h->n_slow + SLOW_TILES_PER_BLOCK - 1) / SLOW_TILES_PER_BLOCK, 1));
+                                         3 * (size_t)std::max((h->n_slow + SWEEP_BY - 1) / SWEEP_BY, 1));
   if ((rc = dev_alloc_t(h, &h->d_partials, nparts))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_counter, 1))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_counter2, 1))) return rc;
@@ -473,7 +500,6 @@ static int one_step(cflbm_handle *h, bool write_macros) {
       sa.mw = h->d_mw;
       sa.mp = h->d_mp;
     }
-    sa.near = h->d_near;
     sa.wall_y = h->cfg.wall_y;
     sa.wall_z = h->cfg.wall_z;
     for (int i = 0; i < Q; ++i) {
@@ -482,6 +508,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
     }
     sa.tile_slow = h->d_tile_slow;
     sa.slow_tiles = h->d_slow_tiles;
+    sa.links_bits = h->d_links_bits;
     sa.n_slow = h->n_slow;
     sa.partials = h->d_partials;
     sa.counter = h->d_counter;

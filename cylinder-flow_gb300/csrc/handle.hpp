@@ -17,7 +17,7 @@ struct cflbm_handle {
   void *fA = nullptr, *fB = nullptr;
   size_t f_bytes = 0;
   uint32_t *d_mask = nullptr;
-  uint32_t *d_near = nullptr;   // solid or next to solid (channel sweep slow path)
+  unsigned *d_links_bits = nullptr;  // link bits of the tiles next to solids
   unsigned char *d_tile_slow = nullptr;  // per warp tile: needs the resolving kernel
   int *d_slow_tiles = nullptr;           // list of those tiles
   int n_slow = 0;

@@ -63,13 +63,13 @@ struct SweepArgs {
   const float *alpha;    // nx*ny*nz Brinkman porosity or null
   double *mu, *mv, *mw, *mp;  // macroscopic output (interior, x fastest) or null
   // Channel profile (boundaries resolved inside the sweep):
-  const uint32_t *near;  // bit-packed: cell is solid or has a solid neighbour
   int wall_y, wall_z;
   double f_in[27];       // inlet equilibrium populations (p = 0, u = (u_in, 0, 0))
   float f_in_f[27];      // the same in FP32 (FP32-arithmetic sweeps)
-  const unsigned char *tile_slow;  // per warp tile (32 cells of a row): 1 = resolve
-  const int *slow_tiles; // list of resolving tiles (tile = (z*ny + y)*nxw + x/32)
+  const unsigned char *tile_slow;  // per warp tile (32 cells of a row): 1 = next to a solid
+  const int *slow_tiles; // list of tiles next to solids (tile = (z*ny + y)*nxw + x/32)
   int n_slow;            // length of the list
+  const unsigned *links_bits;  // per listed tile, 32 cells: bit i = source of i is solid
   double *partials;      // 3 doubles per block of the resolving kernel
   unsigned int *counter; // finished force blocks (self-resetting)
   double *hist;          // force history, 3 doubles per step
@@ -119,10 +119,9 @@ struct ReduceArgs {
 cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cudaStream_t s);
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
                                  cudaStream_t s);
-// Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z;
-// the resolving channel kernel runs 4 warp tiles per block.
+// Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z
+// (the solid-tile launch runs 4 listed warp tiles per block).
 constexpr int SWEEP_BX = 32, SWEEP_BY = 4;
-constexpr int SLOW_TILES_PER_BLOCK = 4;
 cudaError_t launch_fill_channel(int Q, int store, const FillArgs &a, cudaStream_t s);
 cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaStream_t s);
 cudaError_t launch_ghost_copy(int Q, int store, const Layout &L, const void *src, void *dst,

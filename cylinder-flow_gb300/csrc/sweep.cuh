@@ -19,13 +19,12 @@
 //                            were filled by the boundary passes, so the pull is
 //                            plain; applies the reference's inlet/outlet
 //                            overrides of Update.
-//   sweep_fast_kernel     -- channel profile, warp tiles away from the y/z faces
-//                            and from solids: plain pull, inlet/outlet by select.
-//   sweep_resolve_kernel  -- channel profile, the remaining warp tiles (listed):
-//                            resolves every source in the kernel and reduces the
-//                            momentum-exchange force on the body.
-// Splitting the channel sweep keeps the resolving code's registers out of the
-// kernel that does 95%+ of the cells.
+//   sweep_channel_kernel  -- channel profile, in two launches: <SOLID=false>
+//                            over every warp tile not next to a solid (box faces
+//                            resolved by warp-uniform selects), <SOLID=true> over
+//                            the listed tiles next to solids (per-cell link bits,
+//                            body-force reduction).  Keeping the force code out of
+//                            the first launch holds it at 64 registers.
 #pragma once
 #include <utility>
 #include "solver.cuh"
@@ -173,133 +172,125 @@ __device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
   if constexpr (sizeof(A) == 8) return a.f_in[i]; else return a.f_in_f[i];
 }
 
-// Interior warp tiles: no y/z face and no solid within one lattice step, so the
-// pull is plain; the inlet column takes the inlet equilibrium and the outlet
-// column repeats itself (zero gradient) through selects.
-template <int Q, class ST, class A, int MINB>
-__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_fast_kernel(const SweepArgs a) {
+// Post-stream population I of cell X (offset c) in the channel profile.  The
+// source S = X - e_I is mapped onto the box with warp-uniform selects:
+//   z face: periodic -> wrap; free-slip -> mirror (population mirror_z(I),
+//           S.z = X.z); no-slip -> halfway bounce-back f*_{opp(I)}(X);
+//   y face: the same;
+//   x < 0:  inlet equilibrium; x >= nx: zero gradient (S.x = nx - 1);
+//   solid S (bit I of `links`, precomputed for tiles next to solids):
+//           halfway bounce-back f*_{opp(I)}(X), and `hit` is set.
+template <int Q, class ST, class A, int I>
+__device__ __forceinline__ A pull_channel(const typename Store<ST>::elem *__restrict__ fa,
+                                          long long c, long long S, int x, int y, int z,
+                                          unsigned links, bool &hit, const SweepArgs &a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
-  using E = typename SF::elem;
-  const int nx = a.L.nx;
-  const int y = blockIdx.y * SWEEP_BY + threadIdx.y;
-  const int z = blockIdx.z;
-  if (y >= a.L.ny) return;
-  if (a.tile_slow[((long long)z * a.L.ny + y) * a.nxw + blockIdx.x]) return;  // warp-uniform
-  const int xr = blockIdx.x * SWEEP_BX + threadIdx.x;
-  const bool valid = xr < nx;
-  const int x = valid ? xr : nx - 1;
-  const long long S = a.L.S;
-  const long long c = a.L.idx(x, y, z);
-  const E *__restrict__ fa = static_cast<const E *>(a.fa);
-  E *__restrict__ fb = static_cast<E *>(a.fb);
-  A f[Q];
-  static_for(
-      [&](auto ic) {
-        constexpr int I = decltype(ic)::value;
-        using Dd = DirC<Q, I>;
-        const long long o = a.L.off(Dd::ex, Dd::ey, Dd::ez);
-        if constexpr (Dd::ex > 0) {
-          f[I] = (x == 0) ? inlet_pop<A>(a, I) : SF::template load<A, L>(fa + I * S + c - o, I);
-        } else if constexpr (Dd::ex < 0) {
-          const long long adj = (x == nx - 1) ? Dd::ex : 0;  // zero-gradient outlet
-          f[I] = SF::template load<A, L>(fa + I * S + c - o + adj, I);
-        } else {
-          f[I] = SF::template load<A, L>(fa + I * S + c - o, I);
-        }
-      },
-      std::make_integer_sequence<int, Q>{});
-  A rho3, ux, uy, uz;
-  moments<L, A>(f, rho3, ux, uy, uz);
-  const long long cell = ((long long)z * a.L.ny + y) * nx + x;
-  finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
+  using Dd = DirC<Q, I>;
+  if constexpr (I == 0) {
+    return SF::template load<A, L>(fa + c, 0);
+  } else {
+    long long src = c - a.L.off(Dd::ex, Dd::ey, Dd::ez);
+    bool my = false, mz = false, bb = false;
+    if constexpr (Dd::ez != 0) {
+      if (Dd::ez > 0 ? (z == 0) : (z == a.L.nz - 1)) {
+        if (a.wall_z == WALL_PERIODIC) src += (Dd::ez > 0 ? 1LL : -1LL) * a.L.nz * a.L.zs;
+        else if (a.wall_z == WALL_FREESLIP) { mz = true; src += Dd::ez * a.L.zs; }
+        else bb = true;
+      }
+    }
+    if constexpr (Dd::ey != 0) {
+      if (!bb && (Dd::ey > 0 ? (y == 0) : (y == a.L.ny - 1))) {
+        if (a.wall_y == WALL_PERIODIC) src += (Dd::ey > 0 ? 1LL : -1LL) * a.L.ny * a.L.rs;
+        else if (a.wall_y == WALL_FREESLIP) { my = true; src += Dd::ey * a.L.rs; }
+        else bb = true;
+      }
+    }
+    if ((links >> I) & 1u) {
+      hit = true;
+      bb = true;
+    }
+    if (bb) return SF::template load<A, L>(fa + Dd::opp * S + c, Dd::opp);
+    const int j = my ? (mz ? Dd::myz : Dd::my) : (mz ? Dd::mz : I);
+    if constexpr (Dd::ex > 0) {
+      if (x == 0) return inlet_pop<A>(a, j);
+    } else if constexpr (Dd::ex < 0) {
+      if (x == a.L.nx - 1) src += Dd::ex;  // zero-gradient outlet
+    }
+    // mirrors keep |e|, so direction I's storage scale applies to j
+    return SF::template load<A, L>(fa + j * S + src, I);
+  }
 }
 
-// Listed warp tiles: every source X - e_i is resolved --
-//   z outside [0,nz): periodic wrap / free-slip mirror (i -> mirror_z(i), source
-//   z := X.z) / no-slip halfway bounce-back (f*_{opp(i)}(X)); then the same in y;
-//   x < 0: inlet equilibrium; x >= nx: zero gradient (x := nx-1); solid source:
-//   halfway bounce-back f*_{opp(i)}(X).
-// Each solid bounce-back at a fluid cell adds its momentum exchange
-// 2 f*_{opp(i)}(X) e_{opp(i)} to the body force (FP64), reduced by warp
-// shuffles, per block, and over blocks by the last block in block order, into
-// the force-history slot of this step.
-template <int Q, class ST, class A, int MINB>
-__global__ void __launch_bounds__(32 * SLOW_TILES_PER_BLOCK, MINB)
-    sweep_resolve_kernel(const SweepArgs a) {
+// Channel sweep.  SOLID = false: every warp tile not next to a solid (flag 0),
+// launched over the whole box; SOLID = true: the listed tiles next to solids,
+// with the per-cell link bits, the solid mask and the body-force reduction:
+// each solid bounce-back at a fluid cell adds 2 f*_{opp(I)}(X) e_{opp(I)}, summed
+// in FP64, reduced by warp shuffles, per block, and over blocks by the last
+// block in block order into the force-history slot of this step.
+template <int Q, class ST, class A, bool SOLID, int MINB>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kernel(const SweepArgs a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
-  const int nx = a.L.nx, ny = a.L.ny, nz = a.L.nz;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long long t = (long long)blockIdx.x * SLOW_TILES_PER_BLOCK + wid;
-  double Fx = 0.0, Fy = 0.0, Fz = 0.0;
-  if (t < a.n_slow) {  // warp-uniform
-    const int tile = a.slow_tiles[t];
-    const int xw = tile % a.nxw;
+  const int nx = a.L.nx, ny = a.L.ny;
+  const int lane = threadIdx.x, wid = threadIdx.y;
+  int x, y, z;
+  bool active;
+  long long t = 0;
+  if constexpr (SOLID) {
+    t = (long long)blockIdx.x * SWEEP_BY + wid;
+    active = t < a.n_slow;
+    const int tile = active ? a.slow_tiles[t] : 0;
     const int row = tile / a.nxw;
-    const int y = row % ny, z = row / ny;
-    const int xr = xw * 32 + lane;
-    const bool valid = xr < nx;
-    const int x = valid ? xr : nx - 1;
+    y = row % ny;
+    z = row / ny;
+    x = (tile % a.nxw) * SWEEP_BX + lane;
+  } else {
+    y = blockIdx.y * SWEEP_BY + wid;
+    z = blockIdx.z;
+    x = blockIdx.x * SWEEP_BX + lane;
+    active = y < ny && !a.tile_slow[((long long)z * ny + (y < ny ? y : 0)) * a.nxw + blockIdx.x];
+    if (!active) return;  // whole warp
+  }
+  double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+  if (active) {  // warp-uniform
+    const bool valid = x < nx;
+    if (!valid) x = nx - 1;
     const long long S = a.L.S;
     const long long c = a.L.idx(x, y, z);
     const E *__restrict__ fa = static_cast<const E *>(a.fa);
     E *__restrict__ fb = static_cast<E *>(a.fb);
-    const bool solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
+    unsigned links = 0u;
+    bool solid_here = false;
+    if constexpr (SOLID) {
+      links = a.links_bits[t * SWEEP_BX + lane];
+      solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
+    }
     A f[Q];
+    bool hits[Q];
     static_for(
         [&](auto ic) {
           constexpr int I = decltype(ic)::value;
-          using Dd = DirC<Q, I>;
-          if constexpr (I == 0) {
-            f[0] = SF::template load<A, L>(fa + c, 0);
-          } else {
-            int sx = x - Dd::ex, sy = y - Dd::ey, sz = z - Dd::ez;
-            bool my = false, mz = false, bb = false, hit = false;
-            if constexpr (Dd::ez != 0) {
-              if (sz < 0 || sz >= nz) {
-                if (a.wall_z == WALL_PERIODIC) sz = sz < 0 ? sz + nz : sz - nz;
-                else if (a.wall_z == WALL_FREESLIP) { mz = true; sz = z; }
-                else bb = true;
-              }
-            }
-            if constexpr (Dd::ey != 0) {
-              if (!bb && (sy < 0 || sy >= ny)) {
-                if (a.wall_y == WALL_PERIODIC) sy = sy < 0 ? sy + ny : sy - ny;
-                else if (a.wall_y == WALL_FREESLIP) { my = true; sy = y; }
-                else bb = true;
-              }
-            }
-            A v = A(0);
-            if (!bb) {
-              const int j = my ? (mz ? Dd::myz : Dd::my) : (mz ? Dd::mz : I);
-              if (Dd::ex > 0 && sx < 0) {
-                v = inlet_pop<A>(a, j);
-              } else {
-                if (sx >= nx) sx = nx - 1;
-                if (mask_solid(a.mask, a.nxw, ny, sx, sy, sz)) {
-                  bb = true;
-                  hit = true;
-                } else {
-                  // mirrors keep |e|, so direction I's storage scale applies to j
-                  v = SF::template load<A, L>(fa + j * S + a.L.idx(sx, sy, sz), I);
-                }
-              }
-            }
-            if (bb) {
-              v = SF::template load<A, L>(fa + Dd::opp * S + c, Dd::opp);
-              if (hit && valid && !solid_here) {
-                const double m = 2.0 * static_cast<double>(v);
-                Fx -= m * Dd::ex;
-                Fy -= m * Dd::ey;
-                Fz -= m * Dd::ez;
-              }
-            }
-            f[I] = v;
-          }
+          hits[I] = false;
+          f[I] = pull_channel<Q, ST, A, I>(fa, c, S, x, y, z, links, hits[I], a);
         },
         std::make_integer_sequence<int, Q>{});
+    if constexpr (SOLID) {
+      if (valid && !solid_here) {
+        static_for(
+            [&](auto ic) {
+              constexpr int I = decltype(ic)::value;
+              if (hits[I]) {
+                const double m = 2.0 * static_cast<double>(f[I]);
+                Fx -= m * Lat<Q>::ex(I);
+                Fy -= m * Lat<Q>::ey(I);
+                Fz -= m * Lat<Q>::ez(I);
+              }
+            },
+            std::make_integer_sequence<int, Q>{});
+      }
+    }
     A rho3, ux, uy, uz;
     moments<L, A>(f, rho3, ux, uy, uz);
     if (solid_here) {
@@ -308,63 +299,65 @@ __global__ void __launch_bounds__(32 * SLOW_TILES_PER_BLOCK, MINB)
     const long long cell = ((long long)z * ny + y) * nx + x;
     finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
   }
-
-  // Block partial -> partials[blockIdx.x]; the last block sums all partials.
-  constexpr int NW = SLOW_TILES_PER_BLOCK;
-  __shared__ double sh[3][NW];
-  __shared__ bool last;
-  for (int o = 16; o > 0; o >>= 1) {
-    Fx += __shfl_down_sync(0xffffffffu, Fx, o);
-    Fy += __shfl_down_sync(0xffffffffu, Fy, o);
-    Fz += __shfl_down_sync(0xffffffffu, Fz, o);
-  }
-  if (lane == 0) {
-    sh[0][wid] = Fx;
-    sh[1][wid] = Fy;
-    sh[2][wid] = Fz;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double bx = 0.0, by = 0.0, bz = 0.0;
-    for (int w = 0; w < NW; ++w) { bx += sh[0][w]; by += sh[1][w]; bz += sh[2][w]; }
-    a.partials[3 * blockIdx.x] = bx;
-    a.partials[3 * blockIdx.x + 1] = by;
-    a.partials[3 * blockIdx.x + 2] = bz;
-    __threadfence();
-    last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (last) {
-    __threadfence();
-    const volatile double *p = a.partials;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
-      s0 += p[3 * k];
-      s1 += p[3 * k + 1];
-      s2 += p[3 * k + 2];
-    }
+  if constexpr (SOLID) {
+    // Block partial -> partials[blockIdx.x]; the last block sums all partials.
+    constexpr int NW = SWEEP_BY;
+    const int tid = wid * SWEEP_BX + lane;
+    __shared__ double sh[3][NW];
+    __shared__ bool last;
     for (int o = 16; o > 0; o >>= 1) {
-      s0 += __shfl_down_sync(0xffffffffu, s0, o);
-      s1 += __shfl_down_sync(0xffffffffu, s1, o);
-      s2 += __shfl_down_sync(0xffffffffu, s2, o);
+      Fx += __shfl_down_sync(0xffffffffu, Fx, o);
+      Fy += __shfl_down_sync(0xffffffffu, Fy, o);
+      Fz += __shfl_down_sync(0xffffffffu, Fz, o);
     }
-    __syncthreads();
     if (lane == 0) {
-      sh[0][wid] = s0;
-      sh[1][wid] = s1;
-      sh[2][wid] = s2;
+      sh[0][wid] = Fx;
+      sh[1][wid] = Fy;
+      sh[2][wid] = Fz;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double tx = 0.0, ty = 0.0, tz = 0.0;
-      for (int w = 0; w < NW; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
-      const long long st = *a.step;
-      double *h = a.hist + 3 * (st % a.cap);
-      h[0] = tx;
-      h[1] = ty;
-      h[2] = tz;
-      *a.step = st + 1;
-      *a.counter = 0u;
+    if (tid == 0) {
+      double bx = 0.0, by = 0.0, bz = 0.0;
+      for (int w = 0; w < NW; ++w) { bx += sh[0][w]; by += sh[1][w]; bz += sh[2][w]; }
+      a.partials[3 * blockIdx.x] = bx;
+      a.partials[3 * blockIdx.x + 1] = by;
+      a.partials[3 * blockIdx.x + 2] = bz;
+      __threadfence();
+      last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      const volatile double *p = a.partials;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+      for (unsigned k = tid; k < gridDim.x; k += SWEEP_BX * SWEEP_BY) {
+        s0 += p[3 * k];
+        s1 += p[3 * k + 1];
+        s2 += p[3 * k + 2];
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
+      }
+      __syncthreads();
+      if (lane == 0) {
+        sh[0][wid] = s0;
+        sh[1][wid] = s1;
+        sh[2][wid] = s2;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+        for (int w = 0; w < NW; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
+        const long long st = *a.step;
+        double *h = a.hist + 3 * (st % a.cap);
+        h[0] = tx;
+        h[1] = ty;
+        h[2] = tz;
+        *a.step = st + 1;
+        *a.counter = 0u;
+      }
     }
   }
 }
@@ -373,10 +366,9 @@ template <int Q, class ST, class A, int MINB_FAST, int MINB_SLOW>
 cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s) {
   dim3 block(SWEEP_BX, SWEEP_BY, 1);
   dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
-  sweep_fast_kernel<Q, ST, A, MINB_FAST><<<grid, block, 0, s>>>(a);
-  const int sb = (a.n_slow + SLOW_TILES_PER_BLOCK - 1) / SLOW_TILES_PER_BLOCK;
-  sweep_resolve_kernel<Q, ST, A, MINB_SLOW>
-      <<<sb > 0 ? sb : 1, 32 * SLOW_TILES_PER_BLOCK, 0, s>>>(a);
+  sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+  const int sb = (a.n_slow + SWEEP_BY - 1) / SWEEP_BY;
+  sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
   count_launch(2);
   return cudaGetLastError();
 }
