@@ -52,6 +52,19 @@ class Info(ctypes.Structure):
     ]
 
 
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("graph_steps", ctypes.c_int), ("autotune", ctypes.c_int),
+                ("tile_height", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("instances", ctypes.c_int), ("cells", ctypes.c_int64),
+                ("steps_done", ctypes.c_int64), ("tile_height", ctypes.c_int),
+                ("grid_blocks", ctypes.c_int), ("graph_steps", ctypes.c_int),
+                ("tuned_candidates", ctypes.c_int), ("tuned_step_ms", ctypes.c_double),
+                ("bytes_per_cell_step", ctypes.c_double)]
+
+
 # Every exported entry point with its ctypes signature (argtypes, restype).
 SIGNATURES = {
     "cflbm_config_default": ([ctypes.POINTER(Config)], ctypes.c_int),
@@ -79,6 +92,14 @@ SIGNATURES = {
     "cflbm_domain_sums_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "cflbm_batch_options_default": ([ctypes.POINTER(BatchOptions)], ctypes.c_int),
+    "cflbm_batch_create": ([ctypes.POINTER(Config), ctypes.c_int, ctypes.POINTER(BatchOptions),
+                            ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "cflbm_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "cflbm_batch_step": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "cflbm_batch_synchronize": ([ctypes.c_void_p], ctypes.c_int),
+    "cflbm_batch_handle": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_void_p),
+    "cflbm_batch_get_info": ([ctypes.c_void_p, ctypes.POINTER(BatchInfo)], ctypes.c_int),
     "cflbm_last_error": ([], ctypes.c_char_p),
     "cflbm_launch_count": ([], ctypes.c_int64),
 }

@@ -37,28 +37,21 @@ class Solver:
     }
 
     def __init__(self, **kw):
-        cfg = C.Config()
-        C.check(C.lib.cflbm_config_default(ctypes.byref(cfg)), "cflbm_config_default")
-        keep = []
-        for k, v in kw.items():
-            if k in ("solid", "alpha", "ref_ran"):
-                if v is None:
-                    continue
-                dt = {"solid": np.uint8, "alpha": np.float64, "ref_ran": np.int32}[k]
-                a = np.ascontiguousarray(v, dt)
-                keep.append(a)
-                t = {"solid": ctypes.c_uint8, "alpha": ctypes.c_double,
-                     "ref_ran": ctypes.c_int32}[k]
-                setattr(cfg, k, _ptr(a, t))
-            elif k in self._names and isinstance(v, str):
-                setattr(cfg, k, self._names[k][v.lower()])
-            else:
-                setattr(cfg, k, v)
-        if cfg.lattice == C.D2Q9:
-            cfg.nz = 1
+        cfg, keep = make_config(**kw)
         h = ctypes.c_void_p()
         C.check(C.lib.cflbm_create(ctypes.byref(cfg), ctypes.byref(h)), "cflbm_create")
+        self._init_from(h, cfg, owned=True)
+
+    @classmethod
+    def _wrap(cls, h, cfg):
+        """A view of a handle owned elsewhere (a batch instance)."""
+        obj = cls.__new__(cls)
+        obj._init_from(ctypes.c_void_p(h), cfg, owned=False)
+        return obj
+
+    def _init_from(self, h, cfg, owned):
         self._h = h
+        self._owned = owned
         self.cfg = cfg
         self.Q = cfg.lattice
         self.nx, self.ny, self.nz = cfg.nx, cfg.ny, cfg.nz
@@ -67,7 +60,8 @@ class Solver:
     # -- life cycle ---------------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None):
-            C.lib.cflbm_destroy(self._h)
+            if getattr(self, "_owned", True):
+                C.lib.cflbm_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -172,3 +166,96 @@ def write_tecplot_fields(path: str, u, v, w, p, n: int) -> None:
     C.check(C.lib.cflbm_write_tecplot_fields(path.encode(), dim, shp[2], shp[1], shp[0],
                                              *[_ptr(a) for a in arrs], int(n)),
             "cflbm_write_tecplot_fields")
+
+
+_NAMES = Solver._names
+
+
+def make_config(**kw):
+    """A cflbm_config from keyword arguments (see Solver); returns (cfg, buffers
+    that must stay alive until the handle is created)."""
+    cfg = C.Config()
+    C.check(C.lib.cflbm_config_default(ctypes.byref(cfg)), "cflbm_config_default")
+    keep = []
+    for k, v in kw.items():
+        if k in ("solid", "alpha", "ref_ran"):
+            if v is None:
+                continue
+            dt = {"solid": np.uint8, "alpha": np.float64, "ref_ran": np.int32}[k]
+            a = np.ascontiguousarray(v, dt)
+            keep.append(a)
+            t = {"solid": ctypes.c_uint8, "alpha": ctypes.c_double, "ref_ran": ctypes.c_int32}[k]
+            setattr(cfg, k, _ptr(a, t))
+        elif k in _NAMES and isinstance(v, str):
+            setattr(cfg, k, _NAMES[k][v.lower()])
+        else:
+            setattr(cfg, k, v)
+    if cfg.lattice == C.D2Q9:
+        cfg.nz = 1
+    return cfg, keep
+
+
+class Batch:
+    """Many channel instances advanced together (cflbm_batch_*).
+
+    `configs` is a list of keyword dicts as for Solver (CHANNEL profile, one
+    lattice and storage, FP32 arithmetic).  `instance(k)` returns a Solver view of
+    instance k for results (macros, forces, force_history, get_f, mass)."""
+
+    def __init__(self, configs, graph_steps=100, autotune=True, tile_height=4,
+                 blocks_per_sm=8):
+        cfgs = (C.Config * len(configs))()
+        keep = []
+        for k, kw in enumerate(configs):
+            kw = dict(kw)
+            kw.setdefault("compute", "fp32")
+            c, kp = make_config(**kw)
+            keep.extend(kp)
+            cfgs[k] = c
+        opt = C.BatchOptions()
+        C.check(C.lib.cflbm_batch_options_default(ctypes.byref(opt)), "cflbm_batch_options_default")
+        opt.graph_steps = graph_steps
+        opt.autotune = 1 if autotune else 0
+        opt.tile_height = tile_height
+        opt.blocks_per_sm = blocks_per_sm
+        b = ctypes.c_void_p()
+        C.check(C.lib.cflbm_batch_create(cfgs, len(configs), ctypes.byref(opt), ctypes.byref(b)),
+                "cflbm_batch_create")
+        self._b = b
+        self._cfgs = [cfgs[k] for k in range(len(configs))]
+        self.n = len(configs)
+
+    def step(self, n=1):
+        C.check(C.lib.cflbm_batch_step(self._b, int(n)), "cflbm_batch_step")
+        return self
+
+    def synchronize(self):
+        C.check(C.lib.cflbm_batch_synchronize(self._b), "cflbm_batch_synchronize")
+
+    def instance(self, k) -> Solver:
+        h = C.lib.cflbm_batch_handle(self._b, int(k))
+        if not h:
+            raise IndexError(k)
+        return Solver._wrap(h, self._cfgs[k])
+
+    def info(self) -> C.BatchInfo:
+        i = C.BatchInfo()
+        C.check(C.lib.cflbm_batch_get_info(self._b, ctypes.byref(i)), "cflbm_batch_get_info")
+        return i
+
+    def close(self):
+        if getattr(self, "_b", None):
+            C.lib.cflbm_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -68,6 +68,7 @@ void free_handle(cflbm_handle *h) {
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (cudaGraphExec_t g : h->graph_exec)
     if (g) cudaGraphExecDestroy(g);
+  if (h->ev_sync) cudaEventDestroy(h->ev_sync);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -156,7 +157,8 @@ std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int w = 0; w < nxw; ++w) {
-        bool any = false;
+        // Rows on a y or z face always need the resolving pull.
+        bool any = y == 0 || y == ny - 1 || (nz > 1 && (z == 0 || z == nz - 1));
         for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !any; ++x) {
           const size_t n = ((size_t)z * ny + y) * nx + x;
           any = solid[n] || bits[n];
@@ -272,6 +274,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   h->cfg.nz = nz;
   CK_CUDA(cudaSetDevice(cfg->device));
   CK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK_CUDA(cudaEventCreateWithFlags(&h->ev_sync, cudaEventDisableTiming));
 
   // Layout: ghosts as the profile needs them (the reference's 2 or 3 layers,
   // 1 for the channel), rows padded to 128 bytes with >= 4 spare elements past
@@ -383,8 +386,9 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     }
     CK_CUDA(cudaStreamSynchronize(h->stream));  // host vectors die at scope end
   }
+  // Force partials: one per block of listed tiles, for any tile height >= 1.
   const size_t nparts = std::max<size_t>(4 * (size_t)std::max(h->link_blocks, h->reduce_blocks),
-                                         3 * (size_t)std::max((h->n_slow + SWEEP_BY - 1) / SWEEP_BY, 1));
+                                         3 * (size_t)std::max(h->n_slow, 1));
   if ((rc = dev_alloc_t(h, &h->d_partials, nparts))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_counter, 1))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_counter2, 1))) return rc;
@@ -467,6 +471,45 @@ static int record_event(cflbm_handle *h, size_t *idx) {
   return CFLBM_OK;
 }
 
+extern "C++" {
+namespace cflbm {
+// Arguments of the channel sweep of handle h reading fa and writing fb.
+SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool write_macros) {
+  SweepArgs sa{};
+  sa.L = h->L;
+  sa.fa = fa;
+  sa.fb = fb;
+  sa.mask = h->d_mask;
+  sa.nxw = h->nxw;
+  sa.omega = h->omega;
+  sa.omega_f = (float)h->omega;
+  sa.alpha = h->d_alpha;
+  if (write_macros) {
+    sa.mu = h->d_mu;
+    sa.mv = h->d_mv;
+    sa.mw = h->d_mw;
+    sa.mp = h->d_mp;
+  }
+  sa.wall_y = h->cfg.wall_y;
+  sa.wall_z = h->cfg.wall_z;
+  for (int i = 0; i < h->Q; ++i) {
+    sa.f_in[i] = h->f_in[i];
+    sa.f_in_f[i] = (float)h->f_in[i];
+  }
+  sa.tile_slow = h->d_tile_slow;
+  sa.slow_tiles = h->d_slow_tiles;
+  sa.links_bits = h->d_links_bits;
+  sa.n_slow = h->n_slow;
+  sa.partials = h->d_partials;
+  sa.counter = h->d_counter;
+  sa.hist = h->d_hist;
+  sa.step = h->d_step;
+  sa.cap = h->hist_cap;
+  return sa;
+}
+}  // namespace cflbm
+}  // extern "C++"
+
 static int one_step(cflbm_handle *h, bool write_macros) {
   size_t tb0 = 0, tb1 = 0, ts0 = 0, ts1 = 0;
   int trc;
@@ -485,36 +528,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   fa.f_in = h->d_fin;
   const bool ref = h->cfg.profile != CFLBM_PROFILE_CHANNEL;
   if (!ref) {
-    SweepArgs sa{};
-    sa.L = L;
-    sa.fa = h->fA;
-    sa.fb = h->fB;
-    sa.mask = h->d_mask;
-    sa.nxw = h->nxw;
-    sa.omega = h->omega;
-    sa.omega_f = (float)h->omega;
-    sa.alpha = h->d_alpha;
-    if (write_macros) {
-      sa.mu = h->d_mu;
-      sa.mv = h->d_mv;
-      sa.mw = h->d_mw;
-      sa.mp = h->d_mp;
-    }
-    sa.wall_y = h->cfg.wall_y;
-    sa.wall_z = h->cfg.wall_z;
-    for (int i = 0; i < Q; ++i) {
-      sa.f_in[i] = h->f_in[i];
-      sa.f_in_f[i] = (float)h->f_in[i];
-    }
-    sa.tile_slow = h->d_tile_slow;
-    sa.slow_tiles = h->d_slow_tiles;
-    sa.links_bits = h->d_links_bits;
-    sa.n_slow = h->n_slow;
-    sa.partials = h->d_partials;
-    sa.counter = h->d_counter;
-    sa.hist = h->d_hist;
-    sa.step = h->d_step;
-    sa.cap = h->hist_cap;
+    const SweepArgs sa = channel_args(h, h->fA, h->fB, write_macros);
     if (h->timing && (trc = record_event(h, &ts0))) return trc;
     CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream));
     if (h->timing) {
@@ -582,6 +596,8 @@ static int one_step(cflbm_handle *h, bool write_macros) {
 int cflbm_step(cflbm_handle *h, int nsteps) {
   if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
   if (nsteps < 0) return fail(CFLBM_E_INVALID, "nsteps < 0");
+  if (h->batched)
+    return fail(CFLBM_E_INVALID, "this handle belongs to a batch: step it with cflbm_batch_step");
   CK_CUDA(cudaSetDevice(h->cfg.device));
   int left = nsteps;
   // Long calls replay a captured CUDA graph of GRAPH_STEPS steps (an even count,

@@ -1,0 +1,475 @@
+// Batched channels: many independent channel instances of uneven size and
+// Reynolds number advanced together, one persistent work-list launch per sweep
+// kind per step, replayed from a captured CUDA graph, with the launch shape
+// (tile height, persistent grid size) picked by a timing autotuner at creation.
+//
+// Each instance is an ordinary channel-profile handle (its own buffers, mask,
+// solid-tile list, force history), so every per-instance result call of the C ABI
+// works on cflbm_batch_handle(b, k).  The batch adds:
+//   * a device table of per-instance sweep arguments, one per A/B parity and
+//     macro flag;
+//   * a work list of (instance, tile block) items for the interior launch and
+//     one for the solid-tile launch (blocks of `by` listed tiles of one instance);
+//   * two persistent kernels that walk the lists with a grid-stride loop, copying
+//     the instance's arguments to shared memory per item and running the same
+//     per-cell code as the single-channel sweep (pull_plain/pull_resolved, moments,
+//     finish_cell); the solid kernel reduces each instance's body force into
+//     that instance's history, the last block of the instance summing its
+//     partials in block order.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+#include "handle.hpp"
+#include "sweep.cuh"
+
+namespace cflbm {
+int record_error(int code, const char *msg);
+}
+
+using namespace cflbm;
+
+struct cflbm_batch {
+  std::vector<cflbm_handle *> inst;
+  int Q = 9, storage = 0, compute = 1;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  SweepArgs *d_args = nullptr;       // [inst][parity][macros]
+  int4 *d_work_fast[4] = {nullptr};  // per tile height candidate index
+  int4 *d_work_solid[4] = {nullptr};
+  int n_work_fast[4] = {0}, n_work_solid[4] = {0};
+  int by = 4;            // tuned tile height
+  int grid = 0;          // tuned persistent grid size
+  int sms = 152;
+  int graph_steps = 100;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // per parity
+  int parity = 0;        // 0: every instance reads buf[0]
+  long long steps_done = 0;
+  long long cells = 0;
+  double bytes_per_cell = 0;
+  cudaEvent_t done = nullptr;
+  std::vector<double> tune_ms;  // timing of each candidate (for cflbm_batch_info)
+};
+
+namespace {
+
+constexpr int BY_CANDIDATES[4] = {1, 2, 4, 8};
+
+int bfail(int code, const std::string &msg) { return record_error(code, msg.c_str()); }
+
+#define BCK(call)                                                                        \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return bfail(CFLBM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+template <int Q, class ST, class A, int BY, bool SOLID>
+__global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
+    batch_sweep_kernel(const SweepArgs *__restrict__ args, const int4 *__restrict__ work,
+                       int n_work, int sel) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  __shared__ SweepArgs a;
+  const int lane = threadIdx.x, wid = threadIdx.y, tid = wid * 32 + lane;
+  for (int w = blockIdx.x; w < n_work; w += gridDim.x) {
+    const int4 wk = work[w];  // (instance, x tile, y tile | listed block, z)
+    __syncthreads();
+    {
+      const int *src = reinterpret_cast<const int *>(args + 4 * (long long)wk.x + sel);
+      int *dst = reinterpret_cast<int *>(&a);
+      for (int k = tid; k < (int)(sizeof(SweepArgs) / sizeof(int)); k += 32 * BY) dst[k] = src[k];
+    }
+    __syncthreads();
+    const int nx = a.L.nx, ny = a.L.ny;
+    int x, y, z;
+    bool active;
+    long long t = 0;
+    if constexpr (SOLID) {
+      t = (long long)wk.z * BY + wid;
+      active = t < a.n_slow;
+      const int tile = active ? a.slow_tiles[t] : 0;
+      const int row = tile / a.nxw;
+      y = row % ny;
+      z = row / ny;
+      x = (tile % a.nxw) * 32 + lane;
+    } else {
+      y = wk.z * BY + wid;
+      z = wk.w;
+      x = wk.y * 32 + lane;
+      active = y < ny && !a.tile_slow[((long long)z * ny + (y < ny ? y : 0)) * a.nxw + wk.y];
+    }
+    double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+    if (active) {  // warp-uniform
+      const bool valid = x < nx;
+      if (!valid) x = nx - 1;
+      const long long S = a.L.S;
+      const long long c = a.L.idx(x, y, z);
+      const E *__restrict__ fa = static_cast<const E *>(a.fa);
+      E *__restrict__ fb = static_cast<E *>(a.fb);
+      A f[Q];
+      bool solid_here = false;
+      A Fxa = A(0), Fya = A(0), Fza = A(0);
+      if constexpr (SOLID) {
+        const unsigned links = a.links_bits[t * 32 + lane];
+        solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
+        static_for(
+            [&](auto ic) {
+              constexpr int I = decltype(ic)::value;
+              f[I] = pull_resolved<Q, ST, A, I>(fa, c, S, x, y, z, links, a);
+            },
+            std::make_integer_sequence<int, Q>{});
+        if (valid && !solid_here) cell_force<Q, A>(f, links, Fxa, Fya, Fza);
+        Fx = f2d_bits(Fxa);
+        Fy = f2d_bits(Fya);
+        Fz = f2d_bits(Fza);
+      } else {
+        static_for(
+            [&](auto ic) {
+              constexpr int I = decltype(ic)::value;
+              f[I] = pull_plain<Q, ST, A, I>(fa, c, S, x, a);
+            },
+            std::make_integer_sequence<int, Q>{});
+      }
+      A rho3, ux, uy, uz;
+      moments<L, A>(f, rho3, ux, uy, uz);
+      if (solid_here) {
+        rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
+      }
+      const long long cell = ((long long)z * ny + y) * nx + x;
+      finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
+    }
+    if constexpr (SOLID) {
+      __shared__ double sh[3][BY];
+      __shared__ bool last;
+      for (int o = 16; o > 0; o >>= 1) {
+        Fx += __shfl_down_sync(0xffffffffu, Fx, o);
+        Fy += __shfl_down_sync(0xffffffffu, Fy, o);
+        Fz += __shfl_down_sync(0xffffffffu, Fz, o);
+      }
+      if (lane == 0) {
+        sh[0][wid] = Fx;
+        sh[1][wid] = Fy;
+        sh[2][wid] = Fz;
+      }
+      __syncthreads();
+      const int nblk = a.n_slow > 0 ? (a.n_slow + BY - 1) / BY : 1;
+      if (tid == 0) {
+        double bx = 0.0, byy = 0.0, bz = 0.0;
+        for (int q = 0; q < BY; ++q) { bx += sh[0][q]; byy += sh[1][q]; bz += sh[2][q]; }
+        a.partials[3 * wk.z] = bx;
+        a.partials[3 * wk.z + 1] = byy;
+        a.partials[3 * wk.z + 2] = bz;
+        __threadfence();
+        last = atomicAdd(a.counter, 1u) == (unsigned)(nblk - 1);
+      }
+      __syncthreads();
+      if (last && tid == 0) {
+        __threadfence();
+        const volatile double *p = a.partials;
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+        for (int k = 0; k < nblk; ++k) { tx += p[3 * k]; ty += p[3 * k + 1]; tz += p[3 * k + 2]; }
+        const long long st = *a.step;
+        double *h = a.hist + 3 * (st % a.cap);
+        h[0] = tx;
+        h[1] = ty;
+        h[2] = tz;
+        *a.step = st + 1;
+        *a.counter = 0u;
+      }
+    }
+  }
+}
+
+template <int Q, class ST, int BY>
+cudaError_t launch_batch_t(const cflbm_batch *b, int kind, int sel, int grid, cudaStream_t s) {
+  const int ci = BY == 1 ? 0 : BY == 2 ? 1 : BY == 4 ? 2 : 3;
+  dim3 block(32, BY, 1);
+  if (kind == 0) {
+    if (b->n_work_fast[ci] > 0)
+      batch_sweep_kernel<Q, ST, float, BY, false>
+          <<<std::min(grid, b->n_work_fast[ci]), block, 0, s>>>(b->d_args, b->d_work_fast[ci],
+                                                                b->n_work_fast[ci], sel);
+  } else {
+    batch_sweep_kernel<Q, ST, float, BY, true>
+        <<<std::max(1, std::min(grid, b->n_work_solid[ci])), block, 0, s>>>(
+            b->d_args, b->d_work_solid[ci], b->n_work_solid[ci], sel);
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+template <int Q, class ST>
+cudaError_t launch_batch_st(const cflbm_batch *b, int by, int kind, int sel, int grid,
+                            cudaStream_t s) {
+  switch (by) {
+    case 1: return launch_batch_t<Q, ST, 1>(b, kind, sel, grid, s);
+    case 2: return launch_batch_t<Q, ST, 2>(b, kind, sel, grid, s);
+    case 4: return launch_batch_t<Q, ST, 4>(b, kind, sel, grid, s);
+    default: return launch_batch_t<Q, ST, 8>(b, kind, sel, grid, s);
+  }
+}
+
+cudaError_t launch_batch(const cflbm_batch *b, int by, int kind, int sel, int grid,
+                         cudaStream_t s) {
+  if (b->Q == 9) {
+    if (b->storage == CFLBM_STORE_FP64) return launch_batch_st<9, double>(b, by, kind, sel, grid, s);
+    if (b->storage == CFLBM_STORE_FP32) return launch_batch_st<9, float>(b, by, kind, sel, grid, s);
+    return launch_batch_st<9, F16Dev>(b, by, kind, sel, grid, s);
+  }
+  if (b->storage == CFLBM_STORE_FP64) return launch_batch_st<27, double>(b, by, kind, sel, grid, s);
+  if (b->storage == CFLBM_STORE_FP32) return launch_batch_st<27, float>(b, by, kind, sel, grid, s);
+  return launch_batch_st<27, F16Dev>(b, by, kind, sel, grid, s);
+}
+
+// One batch step: both launches, reading buffer `parity` of every instance.
+int batch_one_step(cflbm_batch *b, int by, int grid, bool macros, bool swap) {
+  const int sel = b->parity * 2 + (macros ? 1 : 0);
+  BCK(launch_batch(b, by, 0, sel, grid, b->stream));
+  BCK(launch_batch(b, by, 1, sel, grid, b->stream));
+  if (swap) {
+    b->parity ^= 1;
+    ++b->steps_done;
+  }
+  return CFLBM_OK;
+}
+
+void free_batch(cflbm_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto g : b->graph)
+    if (g) cudaGraphExecDestroy(g);
+  if (b->d_args) cudaFree(b->d_args);
+  for (int k = 0; k < 4; ++k) {
+    if (b->d_work_fast[k]) cudaFree(b->d_work_fast[k]);
+    if (b->d_work_solid[k]) cudaFree(b->d_work_solid[k]);
+  }
+  if (b->done) cudaEventDestroy(b->done);
+  for (auto *h : b->inst) cflbm_destroy(h);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+// Make every instance handle's stream wait for the batch's work so far.
+int publish(cflbm_batch *b) {
+  BCK(cudaEventRecord(b->done, b->stream));
+  for (auto *h : b->inst) BCK(cudaStreamWaitEvent(h->stream, b->done, 0));
+  return CFLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cflbm_batch_options_default(cflbm_batch_options *o) {
+  if (!o) return bfail(CFLBM_E_INVALID, "options is NULL");
+  std::memset(o, 0, sizeof(*o));
+  o->graph_steps = 100;
+  o->autotune = 1;
+  o->tile_height = 4;
+  o->blocks_per_sm = 8;
+  return CFLBM_OK;
+}
+
+int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_options *opt,
+                       cflbm_batch **out) {
+  if (!cfgs || n <= 0 || !out) return bfail(CFLBM_E_INVALID, "need configs, n > 0 and out");
+  *out = nullptr;
+  cflbm_batch_options o;
+  if (opt) o = *opt; else cflbm_batch_options_default(&o);
+  if (o.graph_steps < 2 || (o.graph_steps & 1))
+    return bfail(CFLBM_E_INVALID, "graph_steps must be even and >= 2");
+  for (int k = 0; k < n; ++k) {
+    if (cfgs[k].profile != CFLBM_PROFILE_CHANNEL)
+      return bfail(CFLBM_E_INVALID, "batched instances must use the CHANNEL profile");
+    if (cfgs[k].lattice != cfgs[0].lattice || cfgs[k].storage != cfgs[0].storage ||
+        cfgs[k].compute != CFLBM_COMPUTE_FP32 || cfgs[k].device != cfgs[0].device)
+      return bfail(CFLBM_E_INVALID,
+                   "batched instances need one lattice, one storage, FP32 arithmetic, one device");
+  }
+  std::unique_ptr<cflbm_batch, void (*)(cflbm_batch *)> bp(new cflbm_batch(), free_batch);
+  cflbm_batch *b = bp.get();
+  b->Q = cfgs[0].lattice;
+  b->storage = cfgs[0].storage;
+  b->device = cfgs[0].device;
+  b->graph_steps = o.graph_steps;
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BCK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+  int sms = 0;
+  BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+  b->sms = sms;
+  for (int k = 0; k < n; ++k) {
+    cflbm_handle *h = nullptr;
+    int rc = cflbm_create(&cfgs[k], &h);
+    if (rc) return rc;
+    h->batched = true;
+    b->inst.push_back(h);
+    b->cells += (long long)h->L.nx * h->L.ny * h->L.nz;
+  }
+  const int es = b->storage == CFLBM_STORE_FP64 ? 8 : b->storage == CFLBM_STORE_FP32 ? 4 : 2;
+  b->bytes_per_cell = 2.0 * b->Q * es + 0.125;
+  // Per-instance arguments: [parity][macros].
+  std::vector<SweepArgs> args((size_t)n * 4);
+  for (int k = 0; k < n; ++k) {
+    cflbm_handle *h = b->inst[k];
+    for (int par = 0; par < 2; ++par)
+      for (int m = 0; m < 2; ++m)
+        args[(size_t)k * 4 + par * 2 + m] =
+            channel_args(h, h->buf[par], h->buf[par ^ 1], m == 1);
+  }
+  BCK(cudaMalloc(&b->d_args, args.size() * sizeof(SweepArgs)));
+  BCK(cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice));
+  // Work lists per tile-height candidate.
+  for (int ci = 0; ci < 4; ++ci) {
+    const int by = BY_CANDIDATES[ci];
+    std::vector<int4> wf, ws;
+    for (int k = 0; k < n; ++k) {
+      const cflbm_handle *h = b->inst[k];
+      const int gx = (h->L.nx + 31) / 32, gy = (h->L.ny + by - 1) / by;
+      for (int z = 0; z < h->L.nz; ++z)
+        for (int yb = 0; yb < gy; ++yb)
+          for (int xb = 0; xb < gx; ++xb) wf.push_back(make_int4(k, xb, yb, z));
+      const int nb = (h->n_slow + by - 1) / by;
+      for (int q = 0; q < std::max(nb, 1); ++q) ws.push_back(make_int4(k, 0, 0, q));
+    }
+    b->n_work_fast[ci] = (int)wf.size();
+    b->n_work_solid[ci] = (int)ws.size();
+    BCK(cudaMalloc(&b->d_work_fast[ci], wf.size() * sizeof(int4)));
+    BCK(cudaMalloc(&b->d_work_solid[ci], ws.size() * sizeof(int4)));
+    BCK(cudaMemcpy(b->d_work_fast[ci], wf.data(), wf.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->d_work_solid[ci], ws.data(), ws.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  }
+  // Launch shape: the autotuner times every (tile height, blocks per SM) pair on
+  // the real state without advancing it (A -> B, no swap), then restores the
+  // force-history counters.
+  b->by = o.tile_height;
+  b->grid = std::max(1, o.blocks_per_sm) * sms;
+  if (o.autotune) {
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int ci = 0; ci < 4; ++ci)
+      for (int bps : {2, 4, 8, 16}) {
+        const int by = BY_CANDIDATES[ci];
+        if (32 * by * bps > 2048) continue;
+        const int grid = bps * sms;
+        int rc = batch_one_step(b, by, grid, false, false);
+        if (rc) return rc;
+        BCK(cudaEventRecord(e0, b->stream));
+        for (int r = 0; r < 5 && rc == CFLBM_OK; ++r) rc = batch_one_step(b, by, grid, false, false);
+        if (rc) return rc;
+        BCK(cudaEventRecord(e1, b->stream));
+        BCK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        BCK(cudaEventElapsedTime(&ms, e0, e1));
+        b->tune_ms.push_back(ms / 5.0f);
+        if (ms < best) {
+          best = ms;
+          b->by = by;
+          b->grid = grid;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto *h : b->inst) {
+      BCK(cudaMemsetAsync(h->d_step, 0, sizeof(long long), b->stream));
+      BCK(cudaMemsetAsync(h->d_hist, 0, 3 * sizeof(double) * h->hist_cap, b->stream));
+    }
+    BCK(cudaStreamSynchronize(b->stream));
+  }
+  *out = bp.release();
+  return CFLBM_OK;
+}
+
+int cflbm_batch_destroy(cflbm_batch *b) {
+  free_batch(b);
+  return CFLBM_OK;
+}
+
+int cflbm_batch_step(cflbm_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return bfail(CFLBM_E_INVALID, "bad arguments");
+  BCK(cudaSetDevice(b->device));
+  // Every instance handle's own stream must be idle-ordered before the batch
+  // writes its buffers.
+  for (auto *h : b->inst) {
+    BCK(cudaEventRecord(h->ev_sync, h->stream));
+    BCK(cudaStreamWaitEvent(b->stream, h->ev_sync, 0));
+  }
+  int left = nsteps;
+  while (left > b->graph_steps) {
+    if (!b->graph[b->parity]) {
+      const int par = b->parity;
+      cudaGraph_t g = nullptr;
+      BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = CFLBM_OK;
+      for (int s = 0; s < b->graph_steps && rc == CFLBM_OK; ++s)
+        rc = batch_one_step(b, b->by, b->grid, false, true);
+      cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      BCK(ec);
+      cudaError_t ei = cudaGraphInstantiate(&b->graph[par], g, 0);
+      cudaGraphDestroy(g);
+      BCK(ei);
+      b->parity = par;  // capture walked the parity through an even number of steps
+      b->steps_done -= b->graph_steps;
+    }
+    BCK(cudaGraphLaunch(b->graph[b->parity], b->stream));
+    count_launch(2LL * b->graph_steps);
+    b->steps_done += b->graph_steps;
+    left -= b->graph_steps;
+  }
+  for (int s = 0; s < left; ++s) {
+    int rc = batch_one_step(b, b->by, b->grid, s == left - 1, true);
+    if (rc) return rc;
+  }
+  // Keep the instance handles' host state in step with the device.
+  for (auto *h : b->inst) {
+    h->fA = h->buf[b->parity];
+    h->fB = h->buf[b->parity ^ 1];
+    h->steps_done = b->steps_done;
+  }
+  return publish(b);
+}
+
+int cflbm_batch_synchronize(cflbm_batch *b) {
+  if (!b) return bfail(CFLBM_E_INVALID, "batch is NULL");
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaStreamSynchronize(b->stream));
+  return CFLBM_OK;
+}
+
+cflbm_handle *cflbm_batch_handle(cflbm_batch *b, int k) {
+  if (!b || k < 0 || k >= (int)b->inst.size()) {
+    bfail(CFLBM_E_INVALID, "instance index out of range");
+    return nullptr;
+  }
+  return b->inst[k];
+}
+
+int cflbm_batch_get_info(cflbm_batch *b, cflbm_batch_info *info) {
+  if (!b || !info) return bfail(CFLBM_E_INVALID, "bad arguments");
+  std::memset(info, 0, sizeof(*info));
+  info->instances = (int)b->inst.size();
+  info->cells = b->cells;
+  info->steps_done = b->steps_done;
+  info->tile_height = b->by;
+  info->grid_blocks = b->grid;
+  info->graph_steps = b->graph_steps;
+  info->bytes_per_cell_step = b->bytes_per_cell;
+  info->tuned_candidates = (int)b->tune_ms.size();
+  double best = 0;
+  for (double t : b->tune_ms) best = (best == 0 || t < best) ? t : best;
+  info->tuned_step_ms = best;
+  return CFLBM_OK;
+}
+
+}  // extern "C"

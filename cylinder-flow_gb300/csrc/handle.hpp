@@ -48,6 +48,8 @@ struct cflbm_handle {
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
   long long launches_per_step = 0;
   bool timing = false;
+  bool batched = false;            // owned and stepped by a cflbm_batch
+  cudaEvent_t ev_sync = nullptr;   // orders this handle's stream before a batch step
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<std::pair<size_t, size_t>> sweep_ev, bnd_ev;
@@ -68,6 +70,9 @@ int ref3d_setup(int nx, int ny, int nz, double u0, const int32_t *ran, RefSetup 
 // Channel mask from the configured geometry (reference_setup.cpp).
 void channel_mask(const cflbm_config &c, std::vector<uint8_t> &solid);
 double channel_area(const cflbm_config &c);
+
+// Channel-sweep arguments of a handle (api.cu).
+SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool write_macros);
 
 // Tecplot binary writer (tecplot.cpp).
 int write_tecplot(const char *path, int dim, int nx, int ny, int nz, const double *u,

@@ -19,12 +19,13 @@
 //                            were filled by the boundary passes, so the pull is
 //                            plain; applies the reference's inlet/outlet
 //                            overrides of Update.
-//   sweep_channel_kernel  -- channel profile, in two launches: <SOLID=false>
-//                            over every warp tile not next to a solid (box faces
-//                            resolved by warp-uniform selects), <SOLID=true> over
-//                            the listed tiles next to solids (per-cell link bits,
-//                            body-force reduction).  Keeping the force code out of
-//                            the first launch holds it at 64 registers.
+//   sweep_channel_kernel  -- channel profile, in two launches: <false> over
+//                            every warp tile away from the y/z faces and from
+//                            solids (plain pulls), <true> over the listed face-row
+//                            and solid-adjacent tiles (resolved pulls, per-cell
+//                            link bits, body-force reduction).  Keeping the
+//                            boundary code out of the first launch holds it at
+//                            64 registers with all loads independent.
 #pragma once
 #include <utility>
 #include "solver.cuh"
@@ -172,18 +173,37 @@ __device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
   if constexpr (sizeof(A) == 8) return a.f_in[i]; else return a.f_in_f[i];
 }
 
-// Post-stream population I of cell X (offset c) in the channel profile.  The
-// source S = X - e_I is mapped onto the box with warp-uniform selects:
+// Post-stream population I of cell X (offset c) for rows away from the y/z
+// faces and cells away from solids: the plain pull, with the inlet column
+// taking the inlet equilibrium and the outlet column repeating itself (zero
+// gradient).  Branch-free: the load is always issued (at x = 0 it reads the
+// ghost column) so all Q loads of a cell can be in flight together.
+template <int Q, class ST, class A, int I>
+__device__ __forceinline__ A pull_plain(const typename Store<ST>::elem *__restrict__ fa,
+                                        long long c, long long S, int x, const SweepArgs &a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using Dd = DirC<Q, I>;
+  long long src = c - a.L.off(Dd::ex, Dd::ey, Dd::ez);
+  if constexpr (Dd::ex < 0) src += (x == a.L.nx - 1) ? Dd::ex : 0;
+  A v = SF::template load<A, L>(fa + I * S + src, I);
+  if constexpr (Dd::ex > 0) v = (x == 0) ? inlet_pop<A>(a, I) : v;
+  return v;
+}
+
+// Post-stream population I of cell X for any cell: the source S = X - e_I is
+// mapped onto the box --
 //   z face: periodic -> wrap; free-slip -> mirror (population mirror_z(I),
 //           S.z = X.z); no-slip -> halfway bounce-back f*_{opp(I)}(X);
 //   y face: the same;
 //   x < 0:  inlet equilibrium; x >= nx: zero gradient (S.x = nx - 1);
-//   solid S (bit I of `links`, precomputed for tiles next to solids):
-//           halfway bounce-back f*_{opp(I)}(X), and `hit` is set.
+//   solid S (bit I of `links`): halfway bounce-back f*_{opp(I)}(X).
+// Written with selects on the address and population, so the load is
+// unconditional and independent of the other directions' loads.
 template <int Q, class ST, class A, int I>
-__device__ __forceinline__ A pull_channel(const typename Store<ST>::elem *__restrict__ fa,
-                                          long long c, long long S, int x, int y, int z,
-                                          unsigned links, bool &hit, const SweepArgs &a) {
+__device__ __forceinline__ A pull_resolved(const typename Store<ST>::elem *__restrict__ fa,
+                                           long long c, long long S, int x, int y, int z,
+                                           unsigned links, const SweepArgs &a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using Dd = DirC<Q, I>;
@@ -193,42 +213,57 @@ __device__ __forceinline__ A pull_channel(const typename Store<ST>::elem *__rest
     long long src = c - a.L.off(Dd::ex, Dd::ey, Dd::ez);
     bool my = false, mz = false, bb = false;
     if constexpr (Dd::ez != 0) {
-      if (Dd::ez > 0 ? (z == 0) : (z == a.L.nz - 1)) {
-        if (a.wall_z == WALL_PERIODIC) src += (Dd::ez > 0 ? 1LL : -1LL) * a.L.nz * a.L.zs;
-        else if (a.wall_z == WALL_FREESLIP) { mz = true; src += Dd::ez * a.L.zs; }
-        else bb = true;
-      }
+      const bool out = Dd::ez > 0 ? (z == 0) : (z == a.L.nz - 1);
+      const bool per = out && a.wall_z == WALL_PERIODIC;
+      mz = out && a.wall_z == WALL_FREESLIP;
+      bb = out && a.wall_z == WALL_NOSLIP;
+      src += per ? (Dd::ez > 0 ? 1LL : -1LL) * a.L.nz * a.L.zs : 0LL;
+      src += mz ? (long long)Dd::ez * a.L.zs : 0LL;
     }
     if constexpr (Dd::ey != 0) {
-      if (!bb && (Dd::ey > 0 ? (y == 0) : (y == a.L.ny - 1))) {
-        if (a.wall_y == WALL_PERIODIC) src += (Dd::ey > 0 ? 1LL : -1LL) * a.L.ny * a.L.rs;
-        else if (a.wall_y == WALL_FREESLIP) { my = true; src += Dd::ey * a.L.rs; }
-        else bb = true;
-      }
+      const bool out = !bb && (Dd::ey > 0 ? (y == 0) : (y == a.L.ny - 1));
+      const bool per = out && a.wall_y == WALL_PERIODIC;
+      my = out && a.wall_y == WALL_FREESLIP;
+      bb = bb || (out && a.wall_y == WALL_NOSLIP);
+      src += per ? (Dd::ey > 0 ? 1LL : -1LL) * a.L.ny * a.L.rs : 0LL;
+      src += my ? (long long)Dd::ey * a.L.rs : 0LL;
     }
-    if ((links >> I) & 1u) {
-      hit = true;
-      bb = true;
-    }
-    if (bb) return SF::template load<A, L>(fa + Dd::opp * S + c, Dd::opp);
+    bb = bb || ((links >> I) & 1u);
     const int j = my ? (mz ? Dd::myz : Dd::my) : (mz ? Dd::mz : I);
-    if constexpr (Dd::ex > 0) {
-      if (x == 0) return inlet_pop<A>(a, j);
-    } else if constexpr (Dd::ex < 0) {
-      if (x == a.L.nx - 1) src += Dd::ex;  // zero-gradient outlet
-    }
-    // mirrors keep |e|, so direction I's storage scale applies to j
-    return SF::template load<A, L>(fa + j * S + src, I);
+    if constexpr (Dd::ex < 0) src += (x == a.L.nx - 1) ? Dd::ex : 0;  // zero gradient
+    // mirrors keep |e|, so direction I's storage scale applies to j and opp(I)
+    const long long addr = bb ? (long long)Dd::opp * S + c : (long long)j * S + src;
+    A v = SF::template load<A, L>(fa + addr, I);
+    if constexpr (Dd::ex > 0) v = (!bb && x == 0) ? inlet_pop<A>(a, j) : v;
+    return v;
   }
 }
 
-// Channel sweep.  SOLID = false: every warp tile not next to a solid (flag 0),
-// launched over the whole box; SOLID = true: the listed tiles next to solids,
-// with the per-cell link bits, the solid mask and the body-force reduction:
-// each solid bounce-back at a fluid cell adds 2 f*_{opp(I)}(X) e_{opp(I)}, summed
-// in FP64, reduced by warp shuffles, per block, and over blocks by the last
-// block in block order into the force-history slot of this step.
-template <int Q, class ST, class A, bool SOLID, int MINB>
+// Force of one cell's solid bounce-backs, summed in the arithmetic type (at most
+// Q - 1 terms): each adds 2 f*_{opp(I)}(X) e_{opp(I)} = -2 v_I e_I.
+template <int Q, class A>
+__device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A &fy, A &fz) {
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        if constexpr (I > 0) {
+          const A m = ((links >> I) & 1u) ? A(2) * f[I] : A(0);
+          if constexpr (Lat<Q>::ex(I) != 0) fx -= Lat<Q>::ex(I) * m;
+          if constexpr (Lat<Q>::ey(I) != 0) fy -= Lat<Q>::ey(I) * m;
+          if constexpr (Lat<Q>::ez(I) != 0) fz -= Lat<Q>::ez(I) * m;
+        }
+      },
+      std::make_integer_sequence<int, Q>{});
+}
+
+// Channel sweep.  BOUNDARY = false: every warp tile that is not listed (rows
+// away from the y/z faces, no solid within one step), launched over the whole
+// box, plain pulls.  BOUNDARY = true: the listed tiles (face rows and tiles next
+// to solids), resolved pulls, solid mask, and the body force: per-cell sums in
+// the arithmetic type, accumulated over cells in FP64 -- warp shuffles, per
+// block, then over blocks by the last block in block order -- into the
+// force-history slot of this step.
+template <int Q, class ST, class A, bool BOUNDARY, int MINB>
 __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kernel(const SweepArgs a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
@@ -238,7 +273,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
   int x, y, z;
   bool active;
   long long t = 0;
-  if constexpr (SOLID) {
+  if constexpr (BOUNDARY) {
     t = (long long)blockIdx.x * SWEEP_BY + wid;
     active = t < a.n_slow;
     const int tile = active ? a.slow_tiles[t] : 0;
@@ -253,7 +288,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
     active = y < ny && !a.tile_slow[((long long)z * ny + (y < ny ? y : 0)) * a.nxw + blockIdx.x];
     if (!active) return;  // whole warp
   }
-  double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+  A Fx = A(0), Fy = A(0), Fz = A(0);
   if (active) {  // warp-uniform
     const bool valid = x < nx;
     if (!valid) x = nx - 1;
@@ -261,35 +296,25 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
     const long long c = a.L.idx(x, y, z);
     const E *__restrict__ fa = static_cast<const E *>(a.fa);
     E *__restrict__ fb = static_cast<E *>(a.fb);
-    unsigned links = 0u;
-    bool solid_here = false;
-    if constexpr (SOLID) {
-      links = a.links_bits[t * SWEEP_BX + lane];
-      solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
-    }
     A f[Q];
-    bool hits[Q];
-    static_for(
-        [&](auto ic) {
-          constexpr int I = decltype(ic)::value;
-          hits[I] = false;
-          f[I] = pull_channel<Q, ST, A, I>(fa, c, S, x, y, z, links, hits[I], a);
-        },
-        std::make_integer_sequence<int, Q>{});
-    if constexpr (SOLID) {
-      if (valid && !solid_here) {
-        static_for(
-            [&](auto ic) {
-              constexpr int I = decltype(ic)::value;
-              if (hits[I]) {
-                const double m = 2.0 * static_cast<double>(f[I]);
-                Fx -= m * Lat<Q>::ex(I);
-                Fy -= m * Lat<Q>::ey(I);
-                Fz -= m * Lat<Q>::ez(I);
-              }
-            },
-            std::make_integer_sequence<int, Q>{});
-      }
+    bool solid_here = false;
+    if constexpr (BOUNDARY) {
+      const unsigned links = a.links_bits[t * SWEEP_BX + lane];
+      solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
+      static_for(
+          [&](auto ic) {
+            constexpr int I = decltype(ic)::value;
+            f[I] = pull_resolved<Q, ST, A, I>(fa, c, S, x, y, z, links, a);
+          },
+          std::make_integer_sequence<int, Q>{});
+      if (valid && !solid_here) cell_force<Q, A>(f, links, Fx, Fy, Fz);
+    } else {
+      static_for(
+          [&](auto ic) {
+            constexpr int I = decltype(ic)::value;
+            f[I] = pull_plain<Q, ST, A, I>(fa, c, S, x, a);
+          },
+          std::make_integer_sequence<int, Q>{});
     }
     A rho3, ux, uy, uz;
     moments<L, A>(f, rho3, ux, uy, uz);
@@ -299,21 +324,32 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
     const long long cell = ((long long)z * ny + y) * nx + x;
     finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
   }
-  if constexpr (SOLID) {
-    // Block partial -> partials[blockIdx.x]; the last block sums all partials.
+  if constexpr (BOUNDARY) {
+    // Per-thread FP32/FP64 partials -> FP64; block partial -> partials[blockIdx.x];
+    // the last block sums all partials.
+    double dx, dy, dz;
+    if constexpr (sizeof(A) == 4) {
+      dx = f2d_bits(Fx);
+      dy = f2d_bits(Fy);
+      dz = f2d_bits(Fz);
+    } else {
+      dx = Fx;
+      dy = Fy;
+      dz = Fz;
+    }
     constexpr int NW = SWEEP_BY;
     const int tid = wid * SWEEP_BX + lane;
     __shared__ double sh[3][NW];
     __shared__ bool last;
     for (int o = 16; o > 0; o >>= 1) {
-      Fx += __shfl_down_sync(0xffffffffu, Fx, o);
-      Fy += __shfl_down_sync(0xffffffffu, Fy, o);
-      Fz += __shfl_down_sync(0xffffffffu, Fz, o);
+      dx += __shfl_down_sync(0xffffffffu, dx, o);
+      dy += __shfl_down_sync(0xffffffffu, dy, o);
+      dz += __shfl_down_sync(0xffffffffu, dz, o);
     }
     if (lane == 0) {
-      sh[0][wid] = Fx;
-      sh[1][wid] = Fy;
-      sh[2][wid] = Fz;
+      sh[0][wid] = dx;
+      sh[1][wid] = dy;
+      sh[2][wid] = dz;
     }
     __syncthreads();
     if (tid == 0) {

@@ -171,6 +171,51 @@ int cflbm_write_tecplot_fields(const char *path, int dim, int nx, int ny, int nz
                                const double *u, const double *v, const double *w,
                                const double *p, int n);
 
+/* ---- batched channels ------------------------------------------------------
+ * Many independent CHANNEL-profile instances (uneven sizes, Reynolds numbers)
+ * advanced together: per step one persistent work-list launch over every
+ * instance's interior tiles and one over every instance's solid-adjacent tiles,
+ * replayed from a captured CUDA graph of graph_steps steps; the tile height and
+ * persistent grid size are picked at creation by timing every candidate on the
+ * real state (which is left unchanged).  The reference runs one channel per
+ * process; this has no counterpart there beyond the per-instance physics of
+ * LBM::Collision/Streaming/Update.  All instances share lattice, storage and
+ * device, and use FP32 arithmetic. */
+typedef struct cflbm_batch cflbm_batch;
+
+typedef struct cflbm_batch_options {
+  int graph_steps;    /* steps per captured graph (even, default 100) */
+  int autotune;       /* 1 (default): time candidates at creation */
+  int tile_height;    /* rows per block when not autotuning: 1, 2, 4 or 8 */
+  int blocks_per_sm;  /* persistent grid = SMs * this when not autotuning */
+} cflbm_batch_options;
+
+typedef struct cflbm_batch_info {
+  int instances;
+  int64_t cells;               /* interior cells over all instances */
+  int64_t steps_done;
+  int tile_height;             /* chosen launch shape */
+  int grid_blocks;
+  int graph_steps;
+  int tuned_candidates;        /* launch shapes timed by the autotuner */
+  double tuned_step_ms;        /* best candidate's step time */
+  double bytes_per_cell_step;  /* algorithmic HBM bytes per cell update */
+} cflbm_batch_info;
+
+int cflbm_batch_options_default(cflbm_batch_options *opt);
+/* Create n instances from cfgs[0..n-1] (each as cflbm_create would). */
+int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_options *opt,
+                       cflbm_batch **out);
+int cflbm_batch_destroy(cflbm_batch *b);
+/* Advance every instance nsteps steps (asynchronous). */
+int cflbm_batch_step(cflbm_batch *b, int nsteps);
+int cflbm_batch_synchronize(cflbm_batch *b);
+/* Instance k as a handle for the result calls (macros, forces, force history,
+ * mass, get_f, write_tecplot); stepping it alone is rejected.  Owned by the
+ * batch.  NULL if k is out of range. */
+cflbm_handle *cflbm_batch_handle(cflbm_batch *b, int k);
+int cflbm_batch_get_info(cflbm_batch *b, cflbm_batch_info *info);
+
 /* The CUDA stream (cudaStream_t) the handle launches on, for callers that
  * order their own work or events against the solver. */
 int cflbm_get_stream(cflbm_handle *h, void **stream);
