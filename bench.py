@@ -140,13 +140,8 @@ def barrier(world):
 
 
 def max_over_ranks(x: float, world: int) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from cflbm.replicas import max_over_ranks as _m
+    return _m(x, world)
 
 
 def time_device(solver, steps, warmup):
@@ -225,12 +220,12 @@ def run_gb300(args):
     # ---- the other storage/arithmetic forms at the same grid ---------------------
     extra = {}
     if not args.quick:
-        for name, st, cp, lay in (("fp64_arith", "fp64", "fp64", "soa"),
-                                  ("fp64_store_rows", "fp64", "fp32", "rows"),
-                                  ("fp32_store", "fp32", "fp32", "soa"),
-                                  ("fp32_store_rows", "fp32", "fp32", "rows"),
-                                  ("fp16dev_store", "fp16dev", "fp32", "soa"),
-                                  ("fp16dev_store_rows", "fp16dev", "fp32", "rows")):
+        for name, st, cp, lay in (("fp64_arith", "fp64", "fp64", "rows"),
+                                  ("fp64_store_soa", "fp64", "fp32", "soa"),
+                                  ("fp32_store", "fp32", "fp32", "rows"),
+                                  ("fp32_store_soa", "fp32", "fp32", "soa"),
+                                  ("fp16dev_store", "fp16dev", "fp32", "rows"),
+                                  ("fp16dev_store_soa", "fp16dev", "fp32", "soa")):
             v = variant_mlups(cflbm, local, st, cp, lay,
                               max(steps // 5, 20) if cp == "fp64" else steps // 2,
                               min(warmup, 5))
@@ -386,7 +381,7 @@ def main():
     ap.add_argument("--nz", type=int, default=NZ)
     ap.add_argument("--storage", default="fp64", choices=["fp64", "fp32", "fp16dev"])
     ap.add_argument("--compute", default="fp32", choices=["fp64", "fp32"])
-    ap.add_argument("--layout", default="soa", choices=["soa", "rows"])
+    ap.add_argument("--layout", default="rows", choices=["soa", "rows"])
     args = ap.parse_args()
     args.steps_ref = 1
     if args.warmup < 3:

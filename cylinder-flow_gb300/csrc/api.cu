@@ -253,6 +253,7 @@ int cflbm_config_default(cflbm_config *c) {
   c->u0 = 0.05;
   c->geom = CFLBM_GEOM_NONE;
   c->seed = 1234;
+  c->layout = CFLBM_LAYOUT_ROWS;
   return CFLBM_OK;
 }
 

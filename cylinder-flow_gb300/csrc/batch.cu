@@ -335,7 +335,7 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
         for (int yb = 0; yb < gy; ++yb)
           for (int xb = 0; xb < gx; ++xb) wf.push_back(make_int4(k, xb, yb, z));
       const int nb = (h->n_slow + by - 1) / by;
-      for (int q = 0; q < std::max(nb, 1); ++q) ws.push_back(make_int4(k, 0, 0, q));
+      for (int q = 0; q < std::max(nb, 1); ++q) ws.push_back(make_int4(k, 0, q, 0));  // .z = listed block
     }
     b->n_work_fast[ci] = (int)wf.size();
     b->n_work_solid[ci] = (int)ws.size();

@@ -30,9 +30,9 @@ cudaError_t launch_sweep_channel_q27(int store, int compute, const SweepArgs &a,
     }
   } else {
     switch (store) {
-      case STORE_F64: return launch_sweep_channel_t<27, double, float, 8, 2>(a, s);
-      case STORE_F32: return launch_sweep_channel_t<27, float, float, 8, 2>(a, s);
-      case STORE_F16: return launch_sweep_channel_t<27, F16Dev, float, 8, 2>(a, s);
+      case STORE_F64: return launch_sweep_channel_t<27, double, float, 8, 4>(a, s);
+      case STORE_F32: return launch_sweep_channel_t<27, float, float, 8, 4>(a, s);
+      case STORE_F16: return launch_sweep_channel_t<27, F16Dev, float, 8, 4>(a, s);
     }
   }
   return cudaErrorInvalidValue;

@@ -99,7 +99,7 @@ typedef struct cflbm_info {
 } cflbm_info;
 
 /* Defaults: D2Q9 64x32, FP64 storage and arithmetic, CHANNEL, free-slip y,
- * periodic z, tau0 = 0.03, u0 = 0.05, no body, no perturbation. */
+ * periodic z, tau0 = 0.03, u0 = 0.05, no body, no perturbation, ROWS layout. */
 int cflbm_config_default(cflbm_config *cfg);
 
 /* Allocate device state and initialise it (f = equilibrium of the initial
