@@ -65,6 +65,18 @@ class BatchInfo(ctypes.Structure):
                 ("bytes_per_cell_step", ctypes.c_double)]
 
 
+class AdjointSpec(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int32), ("checkpoint_every", ctypes.c_int32),
+                ("window_begin", ctypes.c_int32), ("window_end", ctypes.c_int32),
+                ("objective", ctypes.c_int32)]
+
+
+class AdjointResult(ctypes.Structure):
+    _fields_ = [("J", ctypes.c_double), ("dJ_du_in", ctypes.c_double),
+                ("dJ_dtau", ctypes.c_double), ("seconds_forward", ctypes.c_double),
+                ("seconds_reverse", ctypes.c_double), ("device_bytes", ctypes.c_int64)]
+
+
 # Every exported entry point with its ctypes signature (argtypes, restype).
 SIGNATURES = {
     "cflbm_config_default": ([ctypes.POINTER(Config)], ctypes.c_int),
@@ -100,6 +112,8 @@ SIGNATURES = {
     "cflbm_batch_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "cflbm_batch_handle": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_void_p),
     "cflbm_batch_get_info": ([ctypes.c_void_p, ctypes.POINTER(BatchInfo)], ctypes.c_int),
+    "cflbm_adjoint": ([ctypes.c_void_p, ctypes.POINTER(AdjointSpec), _dp,
+                       ctypes.POINTER(AdjointResult)], ctypes.c_int),
     "cflbm_last_error": ([], ctypes.c_char_p),
     "cflbm_launch_count": ([], ctypes.c_int64),
 }

@@ -111,6 +111,21 @@ class Solver:
                 "cflbm_force_history")
         return out[: n.value]
 
+    def adjoint(self, steps: int, checkpoint_every: int, window: tuple[int, int],
+                objective: str = "drag"):
+        """cflbm_adjoint on this (fresh) handle: runs `steps` forward steps and the
+        reverse sweep.  Returns J, dJ/dalpha (shape (ny, nx)), dJ/du_in,
+        dJ/dtau and the timings."""
+        spec = C.AdjointSpec(int(steps), int(checkpoint_every), int(window[0]), int(window[1]),
+                             {"drag": 0, "lift": 1}[objective])
+        res = C.AdjointResult()
+        g = np.zeros((self.ny, self.nx))
+        C.check(C.lib.cflbm_adjoint(self._h, ctypes.byref(spec), _ptr(g), ctypes.byref(res)),
+                "cflbm_adjoint")
+        return {"J": res.J, "dJ_dalpha": g, "dJ_du_in": res.dJ_du_in, "dJ_dtau": res.dJ_dtau,
+                "seconds_forward": res.seconds_forward, "seconds_reverse": res.seconds_reverse,
+                "device_bytes": res.device_bytes}
+
     def mass(self):
         m = np.zeros(1)
         mom = np.zeros(3)

@@ -8,6 +8,14 @@ error against the FP64 run, the mean drag coefficient, its error, the lift rms,
 the Strouhal number and the FP64 mass drift.
 
     python -m cflbm.studies precision --nx 768 --ny 384 --nz 384 --steps 20000
+
+adjoint_study: the differentiation problem (D2Q9 1024x256 channel, cylinder
+D=32 at (200, 128), porosity on a 128x128 box, mean drag over steps 5000-7000
+of 7000, checkpoints every 100).  Runs the FP32 and FP64 adjoints, compares
+them, and checks the FP64 gradient against central differences (h = 1e-4) of
+the FP64 solver for u_in, tau and 16 seeded porosity directions.
+
+    python -m cflbm.studies adjoint --out adjoint.json
 """
 from __future__ import annotations
 
@@ -89,9 +97,103 @@ def precision_study(case, steps, window, peak_gbs, forms=FORMS, out_path=None):
     return results
 
 
+def adjoint_case(nx=1024, ny=256, diam=32.0, cx=200.0, cy=128.0, u0=0.05, re=100.0):
+    """The differentiation problem (free-slip walls; tau = 0.5 + 3 u D / Re)."""
+    return dict(lattice=9, nx=nx, ny=ny, geom="cylinder", cx=cx, cy=cy, diam=diam,
+                wall_y="freeslip", perturb_amp=1e-3, seed=1234), u0, 0.5 + 3.0 * u0 * diam / re
+
+
+def adjoint_study(steps=7000, window=(5000, 7000), checkpoint_every=100, box=128,
+                  directions=16, h=1e-4, seed=11, out_path=None, nx=1024, ny=256,
+                  precisions=("fp32", "fp64"), fd=True):
+    from .adjoint import run, smooth_porosity
+    case, u_in, tau = adjoint_case(nx=nx, ny=ny)
+    x0, y0 = int(case["cx"]) - box // 2, int(case["cy"]) - box // 2
+    alpha = smooth_porosity(nx, ny, (x0, y0, x0 + box, y0 + box), seed=seed)
+    alpha = alpha.astype(np.float32).astype(np.float64)  # the solver stores FP32
+    res = {"case": case, "u_in": u_in, "tau": tau, "steps": steps, "window": window,
+           "checkpoint_every": checkpoint_every, "h": h}
+
+    def dump():
+        if out_path:
+            with open(out_path, "w") as fh:
+                json.dump(res, fh, indent=1)
+
+    grads = {}
+    for prec in precisions:
+        c = dict(case, storage=prec, compute=prec)
+        r = run(c, alpha, u_in, tau, steps, checkpoint_every, window)
+        # plain forward step time of the same problem (graph replay, no checkpoints)
+        with Solver(**c, u0=u_in, tau0=tau - 0.5, alpha=alpha, force_history=64) as s:
+            s.step(200)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(2000)
+            s.synchronize()
+            fwd_step = (time.perf_counter() - t0) / 2000
+        grads[prec] = r
+        res[prec] = {"J": r["J"], "dJ_du_in": r["dJ_du_in"], "dJ_dtau": r["dJ_dtau"],
+                     "dJ_dalpha_norm": float(np.linalg.norm(r["dJ_dalpha"])),
+                     "seconds_forward": r["seconds_forward"],
+                     "seconds_reverse": r["seconds_reverse"],
+                     "forward_step_s": fwd_step,
+                     "reverse_step_s": r["seconds_reverse"] / steps,
+                     "reverse_over_forward_step": r["seconds_reverse"] / steps / fwd_step,
+                     "device_bytes": r["device_bytes"]}
+        print(prec, json.dumps(res[prec]), flush=True)
+        dump()
+    if not fd or len(grads) < 2:
+        dump()
+        return res
+    g64, g32 = grads["fp64"], grads["fp32"]
+    res["fp32_vs_fp64"] = {
+        "J_rel": abs(g32["J"] - g64["J"]) / abs(g64["J"]),
+        "dJ_du_in_rel": abs(g32["dJ_du_in"] - g64["dJ_du_in"]) / abs(g64["dJ_du_in"]),
+        "dJ_dtau_rel": abs(g32["dJ_dtau"] - g64["dJ_dtau"]) / abs(g64["dJ_dtau"]),
+        "dJ_dalpha_rel_l2": float(np.linalg.norm(g32["dJ_dalpha"] - g64["dJ_dalpha"]) /
+                                  np.linalg.norm(g64["dJ_dalpha"]))}
+    print("fp32_vs_fp64", json.dumps(res["fp32_vs_fp64"]), flush=True)
+
+    c64 = dict(case, storage="fp64", compute="fp64")
+
+    def J(a, u, t):
+        with Solver(**c64, u0=u, tau0=t - 0.5, alpha=a, force_history=steps) as s:
+            s.step(steps)
+            f = s.force_history(steps)
+        return float(np.mean(f[window[0] - 1:window[1], 0]))
+
+    fd = {}
+    fd["dJ_du_in"] = (J(alpha, u_in + h, tau) - J(alpha, u_in - h, tau)) / (2 * h)
+    fd["dJ_dtau"] = (J(alpha, u_in, tau + h) - J(alpha, u_in, tau - h)) / (2 * h)
+    fd["dJ_du_in_rel_err"] = abs(g64["dJ_du_in"] - fd["dJ_du_in"]) / abs(fd["dJ_du_in"])
+    fd["dJ_dtau_rel_err"] = abs(g64["dJ_dtau"] - fd["dJ_dtau"]) / abs(fd["dJ_dtau"])
+    rng = np.random.default_rng(seed + 1)
+    mask = np.zeros_like(alpha)
+    mask[y0:y0 + box, x0:x0 + box] = 1.0
+    dirs = []
+    for k in range(directions):
+        d = rng.standard_normal(alpha.shape) * mask
+        d /= np.max(np.abs(d))
+        ap = (alpha + h * d).astype(np.float32).astype(np.float64)
+        am = (alpha - h * d).astype(np.float32).astype(np.float64)
+        f = J(ap, u_in, tau) - J(am, u_in, tau)
+        a64 = float(np.sum(g64["dJ_dalpha"] * (ap - am)))
+        a32 = float(np.sum(g32["dJ_dalpha"] * (ap - am)))
+        dirs.append({"fd": f, "adjoint_fp64": a64, "adjoint_fp32": a32,
+                     "rel_err_fp64": abs(a64 - f) / abs(f), "rel_err_fp32": abs(a32 - f) / abs(f)})
+    fd["directions"] = dirs
+    fd["max_rel_err_fp64"] = max(d["rel_err_fp64"] for d in dirs)
+    fd["median_rel_err_fp64"] = float(np.median([d["rel_err_fp64"] for d in dirs]))
+    fd["max_rel_err_fp32"] = max(d["rel_err_fp32"] for d in dirs)
+    res["finite_differences"] = fd
+    print("fd", json.dumps({k: v for k, v in fd.items() if k != "directions"}), flush=True)
+    dump()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision"])
+    ap.add_argument("study", choices=["precision", "adjoint"])
     ap.add_argument("--nx", type=int, default=768)
     ap.add_argument("--ny", type=int, default=384)
     ap.add_argument("--nz", type=int, default=384)
@@ -100,7 +202,20 @@ def main():
     ap.add_argument("--peak", type=float, default=6656.0)
     ap.add_argument("--out", default=None)
     ap.add_argument("--forms", default=",".join(f[0] for f in FORMS))
+    ap.add_argument("--directions", type=int, default=16)
+    ap.add_argument("--checkpoint", type=int, default=100)
+    ap.add_argument("--precisions", default="fp32,fp64")
+    ap.add_argument("--no-fd", action="store_true")
     args = ap.parse_args()
+    if args.study == "adjoint":
+        steps = args.steps if args.steps != 20000 else 7000
+        window = (steps - 2000, steps) if steps > 2000 else (steps // 2, steps)
+        nx = args.nx if args.nx != 768 else 1024
+        ny = args.ny if args.ny != 384 else 256
+        adjoint_study(steps, window, args.checkpoint, directions=args.directions,
+                      out_path=args.out, nx=nx, ny=ny,
+                      precisions=tuple(args.precisions.split(",")), fd=not args.no_fd)
+        return
     keep = set(args.forms.split(","))
     forms = [f for f in FORMS if f[0] in keep]
     case = sphere_case(args.nx, args.ny, args.nz, diam=64.0 * args.nx / 768.0)

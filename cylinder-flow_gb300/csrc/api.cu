@@ -6,6 +6,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 #include "handle.hpp"
 
@@ -69,6 +70,10 @@ void free_handle(cflbm_handle *h) {
   for (cudaGraphExec_t g : h->graph_exec)
     if (g) cudaGraphExecDestroy(g);
   if (h->ev_sync) cudaEventDestroy(h->ev_sync);
+  if (h->fork.side) cudaStreamSynchronize(h->fork.side);
+  if (h->fork.fork) cudaEventDestroy(h->fork.fork);
+  if (h->fork.join) cudaEventDestroy(h->fork.join);
+  if (h->fork.side) cudaStreamDestroy(h->fork.side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -109,37 +114,84 @@ void build_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
       }
 }
 
+// Run body(r) for r in [0, n) on the host's cores (rows are independent).
+template <class F>
+void host_parallel_rows(long long n, F body) {
+  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const long long nt = std::min<long long>(hw, std::max<long long>(1, n / 64));
+  if (nt <= 1) {
+    for (long long r = 0; r < n; ++r) body(r);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (long long t = 0; t < nt; ++t)
+    pool.emplace_back([=, &body] {
+      for (long long r = t; r < n; r += nt) body(r);
+    });
+  for (auto &th : pool) th.join();
+}
+
 // Channel-profile solid links: bit i of cell X is set when the source of
 // population i, X - e_i mapped onto the box exactly as the sweep maps it
 // (periodic wrap / free-slip mirror / no-slip wall / inlet / zero-gradient
 // outlet), is a solid cell -- i.e. when the sweep must bounce population i back.
+// Every source lies within one cell of X in each axis, so only cells within one
+// cell (in x) of a solid of a neighbouring row can have bits: each row scans the
+// x-range spanned by the solids of its (up to 3 x 3) source rows.
 template <int Q>
 std::vector<uint32_t> channel_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
                                     int wall_y, int wall_z) {
   using L = Lat<Q>;
   std::vector<uint32_t> bits(solid.size(), 0u);
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < ny; ++y)
-      for (int x = 0; x < nx; ++x) {
-        uint32_t b = 0u;
-        for (int i = 1; i < Q; ++i) {
-          int sx = x - L::ex(i), sy = y - L::ey(i), sz = z - L::ez(i);
-          if (Q == 27 && (sz < 0 || sz >= nz)) {
-            if (wall_z == CFLBM_WALL_PERIODIC) sz = (sz + nz) % nz;
-            else if (wall_z == CFLBM_WALL_FREESLIP) sz = z;
-            else continue;  // no-slip wall, not the body
-          }
-          if (sy < 0 || sy >= ny) {
-            if (wall_y == CFLBM_WALL_PERIODIC) sy = (sy + ny) % ny;
-            else if (wall_y == CFLBM_WALL_FREESLIP) sy = y;
-            else continue;
-          }
-          if (sx < 0) continue;  // inlet
-          if (sx >= nx) sx = nx - 1;
-          if (solid[((size_t)sz * ny + sy) * nx + sx]) b |= 1u << i;
-        }
-        bits[((size_t)z * ny + y) * nx + x] = b;
+  const long long rows = (long long)ny * nz;
+  std::vector<int> rmin(rows, nx), rmax(rows, -1);
+  host_parallel_rows(rows, [&](long long r) {
+    const uint8_t *row = &solid[(size_t)r * nx];
+    for (int x = 0; x < nx; ++x)
+      if (row[x]) {
+        rmin[r] = std::min(rmin[r], x);
+        rmax[r] = x;
       }
+  });
+  host_parallel_rows(rows, [&](long long r) {
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    int lo = nx, hi = -1;
+    for (int dz = (Q == 27 ? -1 : 0); dz <= (Q == 27 ? 1 : 0); ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int zz = z + dz, yy = y + dy;
+        if (zz < 0 || zz >= nz) {
+          if (wall_z != CFLBM_WALL_PERIODIC) continue;
+          zz = (zz + nz) % nz;
+        }
+        if (yy < 0 || yy >= ny) {
+          if (wall_y != CFLBM_WALL_PERIODIC) continue;
+          yy = (yy + ny) % ny;
+        }
+        const long long q = (long long)zz * ny + yy;
+        lo = std::min(lo, rmin[q]);
+        hi = std::max(hi, rmax[q]);
+      }
+    for (int x = std::max(0, lo - 1); x <= std::min(nx - 1, hi + 1); ++x) {
+      uint32_t b = 0u;
+      for (int i = 1; i < Q; ++i) {
+        int sx = x - L::ex(i), sy = y - L::ey(i), sz = z - L::ez(i);
+        if (Q == 27 && (sz < 0 || sz >= nz)) {
+          if (wall_z == CFLBM_WALL_PERIODIC) sz = (sz + nz) % nz;
+          else if (wall_z == CFLBM_WALL_FREESLIP) sz = z;
+          else continue;  // no-slip wall, not the body
+        }
+        if (sy < 0 || sy >= ny) {
+          if (wall_y == CFLBM_WALL_PERIODIC) sy = (sy + ny) % ny;
+          else if (wall_y == CFLBM_WALL_FREESLIP) sy = y;
+          else continue;
+        }
+        if (sx < 0) continue;  // inlet
+        if (sx >= nx) sx = nx - 1;
+        if (solid[((size_t)sz * ny + sy) * nx + sx]) b |= 1u << i;
+      }
+      bits[((size_t)z * ny + y) * nx + x] = b;
+    }
+  });
   return bits;
 }
 
@@ -276,6 +328,15 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaSetDevice(cfg->device));
   CK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   CK_CUDA(cudaEventCreateWithFlags(&h->ev_sync, cudaEventDisableTiming));
+  if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
+    // Side stream of the channel sweep's listed-tile kernel, at the highest
+    // priority so its blocks are scheduled ahead of the interior kernel's.
+    int lo = 0, hi = 0;
+    CK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CK_CUDA(cudaStreamCreateWithPriority(&h->fork.side, cudaStreamNonBlocking, hi));
+    CK_CUDA(cudaEventCreateWithFlags(&h->fork.fork, cudaEventDisableTiming));
+    CK_CUDA(cudaEventCreateWithFlags(&h->fork.join, cudaEventDisableTiming));
+  }
 
   // Layout: ghosts as the profile needs them (the reference's 2 or 3 layers,
   // 1 for the channel), rows padded to 128 bytes with >= 4 spare elements past
@@ -531,7 +592,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   if (!ref) {
     const SweepArgs sa = channel_args(h, h->fA, h->fB, write_macros);
     if (h->timing && (trc = record_event(h, &ts0))) return trc;
-    CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream));
+    CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream, &h->fork));
     if (h->timing) {
       if ((trc = record_event(h, &ts1))) return trc;
       h->sweep_ev.push_back({ts0, ts1});
@@ -618,7 +679,7 @@ int cflbm_step(cflbm_handle *h, int nsteps) {
         return rc;
       }
       CK_CUDA(ec);
-      cudaError_t ei = cudaGraphInstantiate(&h->graph_exec[par], g, 0);
+      cudaError_t ei = cudaGraphInstantiate(&h->graph_exec[par], g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       CK_CUDA(ei);
       h->launches_per_step = (launches() - n0) / GRAPH_STEPS;

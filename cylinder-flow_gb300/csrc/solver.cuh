@@ -117,8 +117,15 @@ struct ReduceArgs {
 
 // ---- launchers (defined in the .cu files, dispatch on lattice and storage) ----
 cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cudaStream_t s);
+// Fork/join of the two channel-sweep launches: the listed-tile kernel runs on
+// `side` while the interior kernel runs on the main stream (they write disjoint
+// cells and only read the current state), joined before anything that follows.
+struct SweepFork {
+  cudaStream_t side;
+  cudaEvent_t fork, join;
+};
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
-                                 cudaStream_t s);
+                                 cudaStream_t s, const SweepFork *fk = nullptr);
 // Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z
 // (the solid-tile launch runs 4 listed warp tiles per block).
 constexpr int SWEEP_BX = 32, SWEEP_BY = 4;

@@ -399,12 +399,26 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
 }
 
 template <int Q, class ST, class A, int MINB_FAST, int MINB_SLOW>
-cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s) {
+cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const SweepFork *fk) {
   dim3 block(SWEEP_BX, SWEEP_BY, 1);
   dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
-  sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
   const int sb = (a.n_slow + SWEEP_BY - 1) / SWEEP_BY;
-  sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
+  if (fk && fk->side) {
+    // The listed tiles go first on the (higher-priority) side stream, so their
+    // latency-bound blocks overlap the interior kernel's streaming.
+    cudaError_t e = cudaEventRecord(fk->fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(fk->side, fk->fork, 0);
+    if (e != cudaSuccess) return e;
+    sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, fk->side>>>(a);
+    e = cudaEventRecord(fk->join, fk->side);
+    if (e != cudaSuccess) return e;
+    sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+    e = cudaStreamWaitEvent(s, fk->join, 0);
+    if (e != cudaSuccess) return e;
+  } else {
+    sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+    sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
+  }
   count_launch(2);
   return cudaGetLastError();
 }

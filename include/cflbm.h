@@ -253,6 +253,43 @@ int cflbm_domain_sums_noalloc(int lattice, int storage, int nx, int ny, int nz,
                               const void *d_f, const uint8_t *d_solid, double *d_out,
                               void *stream);
 
+/* Discrete adjoint of the D2Q9 channel step -- no counterpart in the reference,
+ * which has no gradients.  It differentiates the step the reference performs in
+ * LBM::Collision and LBM::Streaming ("Kokkos/lbm.cpp:134-186": BGK collision,
+ * pull streaming, halfway bounce-back; momentum-exchange force of
+ * "MPI Kokkos/lbm.cpp:356-377") for the channel profile, with the Brinkman
+ * porosity field of cflbm_config.alpha, free-slip / no-slip / periodic y walls.
+ *
+ * Objective J = mean over steps [window_begin, window_end] (1-based) of F_x
+ * (objective 0, drag) or F_y (1, lift), the force history the solver records.
+ * The call runs `steps` forward steps from a fresh handle (steps_done == 0,
+ * force_history >= steps), keeping a checkpoint every `checkpoint_every` steps,
+ * then runs the reverse sweep segment by segment (recomputing each segment's
+ * states from its checkpoint while the previous one is reversed), so device
+ * memory is ceil(steps/K) + 2K states on top of the handle.  FP32/FP32 or
+ * FP64/FP64 storage/arithmetic.
+ * dJ_dalpha: host, nx*ny doubles (x fastest) or NULL; the gradient with respect
+ * to the per-cell porosity (at alpha = 0 where the handle has no field). */
+typedef struct cflbm_adjoint_spec {
+  int32_t steps;            /* forward steps T */
+  int32_t checkpoint_every; /* K */
+  int32_t window_begin;     /* first step of the averaging window */
+  int32_t window_end;       /* last step of the window (<= T) */
+  int32_t objective;        /* 0: F_x, 1: F_y */
+} cflbm_adjoint_spec;
+
+typedef struct cflbm_adjoint_result {
+  double J;                 /* objective of the forward run */
+  double dJ_du_in;          /* inlet speed (inlet equilibrium and initial u_x) */
+  double dJ_dtau;           /* relaxation time tau = tau0 + 0.5 */
+  double seconds_forward;   /* wall time of the forward run with checkpoints */
+  double seconds_reverse;   /* wall time of recomputation + reverse sweep */
+  int64_t device_bytes;     /* scratch the call allocated */
+} cflbm_adjoint_result;
+
+int cflbm_adjoint(cflbm_handle *h, const cflbm_adjoint_spec *spec, double *dJ_dalpha,
+                  cflbm_adjoint_result *result);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char *cflbm_last_error(void);
 

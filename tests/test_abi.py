@@ -41,6 +41,42 @@ def test_library_exports_every_declared_symbol():
     assert names <= set(C.SIGNATURES)
 
 
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every struct of include/cflbm.h has the size and field offsets the
+    ctypes binding assumes (compiled with the host C compiler)."""
+    structs = {"cflbm_config": C.Config, "cflbm_info": C.Info,
+               "cflbm_batch_options": C.BatchOptions, "cflbm_batch_info": C.BatchInfo,
+               "cflbm_adjoint_spec": C.AdjointSpec, "cflbm_adjoint_result": C.AdjointResult}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cflbm.h"',
+             'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                 check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)
+
+
+def test_smooth_porosity_field():
+    from cflbm.adjoint import smooth_porosity
+    a = smooth_porosity(64, 40, (10, 5, 42, 37), seed=3)
+    b = smooth_porosity(64, 40, (10, 5, 42, 37), seed=3)
+    assert np.array_equal(a, b)
+    assert a.max() == 1.0 and a.min() >= 0.0
+    assert np.all(a[:5] == 0) and np.all(a[37:] == 0) and np.all(a[:, :10] == 0)
+    assert np.all(a[5:37, 10:42] > 0)
+
+
 def test_build_targets_sm103a_only():
     from cflbm import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]

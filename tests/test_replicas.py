@@ -35,7 +35,7 @@ def _worker(rank, world, port, out):
 def test_two_rank_aggregation_uses_slowest_rank():
     import torch.multiprocessing as mp
     world = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
     for r in range(world):
