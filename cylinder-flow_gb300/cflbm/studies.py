@@ -16,6 +16,15 @@ them, and checks the FP64 gradient against central differences (h = 1e-4) of
 the FP64 solver for u_in, tau and 16 seeded porosity directions.
 
     python -m cflbm.studies adjoint --out adjoint.json
+
+batch_study: the batched form (64 D2Q9 cylinder channels, widths 256-1024 and
+heights 64-256 in multiples of 32, D in [8, 32], Re in [40, 200], u_in = 0.05,
+FP32 storage, 20000 steps in one persistent launch per step replayed from a
+100-step CUDA graph, autotuned launch shape) against the same channels run one
+at a time with FP64 storage and arithmetic; per-instance Cd error against that
+FP64 run.
+
+    python -m cflbm.studies batch --out batch.json
 """
 from __future__ import annotations
 
@@ -191,9 +200,88 @@ def adjoint_study(steps=7000, window=(5000, 7000), checkpoint_every=100, box=128
     return res
 
 
+def batch_cases(n=64, seed=2025, u0=0.05):
+    """The batched-form channels: seeded uniform draws of width, height, diameter
+    and Reynolds number; body at (4D, H/2); free-slip walls."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        nx = int(rng.integers(256 // 32, 1024 // 32 + 1)) * 32
+        ny = int(rng.integers(64 // 32, 256 // 32 + 1)) * 32
+        d = float(rng.uniform(8.0, 32.0))
+        re = float(rng.uniform(40.0, 200.0))
+        out.append(dict(lattice=9, nx=nx, ny=ny, tau0=3.0 * u0 * d / re, u0=u0,
+                        wall_y="freeslip", geom="cylinder", cx=4.0 * d, cy=ny / 2.0, diam=d,
+                        perturb_amp=1e-3, seed=1000 + k, re=re))
+    return out
+
+
+def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=6656.0,
+                out_path=None, sequential=True):
+    from .solver import Batch
+    cases = batch_cases(n)
+    cfgs = [{k: v for k, v in c.items() if k != "re"} for c in cases]
+    cells = sum(c["nx"] * c["ny"] for c in cfgs)
+    res = {"instances": n, "steps": steps, "graph_steps": graph_steps, "cells": cells,
+           "cases": cases}
+    t0 = time.perf_counter()
+    with Batch([dict(c, storage="fp32", compute="fp32", force_history=steps + 8)
+                for c in cfgs], graph_steps=graph_steps, autotune=True) as b:
+        t_create = time.perf_counter() - t0
+        b.step(graph_steps)  # first replay captures the graph
+        b.synchronize()
+        t1 = time.perf_counter()
+        b.step(steps - graph_steps)
+        b.synchronize()
+        wall = time.perf_counter() - t1
+        info = b.info()
+        cd32 = []
+        for k, c in enumerate(cfgs):
+            hist = b.instance(k).force_history(steps)
+            cd32.append(analysis.summary(hist, c["u0"], c["diam"], c["diam"], window)["cd_mean"])
+    bpc = info.bytes_per_cell_step
+    res["batch"] = {
+        "create_s": t_create, "wall_s": wall, "timed_steps": steps - graph_steps,
+        "mlups": cells * (steps - graph_steps) / wall / 1e6,
+        "hbm_frac": bpc * cells * (steps - graph_steps) / wall / 1e9 / peak_gbs,
+        "bytes_per_cell_step": bpc, "tile_height": info.tile_height,
+        "grid_blocks": info.grid_blocks, "tuned_candidates": info.tuned_candidates,
+        "tuned_step_ms": info.tuned_step_ms}
+    print("batch", json.dumps(res["batch"]), flush=True)
+    if out_path:
+        with open(out_path, "w") as fh:
+            json.dump(res, fh, indent=1)
+    if not sequential:
+        return res
+    seq_wall = 0.0
+    cd64 = []
+    for k, c in enumerate(cfgs):
+        with Solver(**c, storage="fp64", compute="fp64", force_history=steps + 8) as s:
+            s.synchronize()
+            t = time.perf_counter()
+            s.step(steps)
+            s.synchronize()
+            seq_wall += time.perf_counter() - t
+            hist = s.force_history(steps)
+        cd64.append(analysis.summary(hist, c["u0"], c["diam"], c["diam"], window)["cd_mean"])
+    err = [abs(a - b) / abs(b) for a, b in zip(cd32, cd64)]
+    res["sequential_fp64"] = {
+        "wall_s": seq_wall, "mlups": cells * steps / seq_wall / 1e6,
+        "hbm_frac": 144.0 * cells * steps / seq_wall / 1e9 / peak_gbs}
+    res["speedup"] = res["batch"]["mlups"] / res["sequential_fp64"]["mlups"]
+    res["cd"] = {"fp32_batch": cd32, "fp64_sequential": cd64, "rel_err": err,
+                 "max_rel_err": max(err), "median_rel_err": float(np.median(err))}
+    print("sequential_fp64", json.dumps(res["sequential_fp64"]), flush=True)
+    print("cd", json.dumps({k: v for k, v in res["cd"].items() if "err" in k}), flush=True)
+    if out_path:
+        with open(out_path, "w") as fh:
+            json.dump(res, fh, indent=1)
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "adjoint"])
+    ap.add_argument("study", choices=["precision", "adjoint", "batch"])
     ap.add_argument("--nx", type=int, default=768)
     ap.add_argument("--ny", type=int, default=384)
     ap.add_argument("--nz", type=int, default=384)
@@ -206,7 +294,13 @@ def main():
     ap.add_argument("--checkpoint", type=int, default=100)
     ap.add_argument("--precisions", default="fp32,fp64")
     ap.add_argument("--no-fd", action="store_true")
+    ap.add_argument("--instances", type=int, default=64)
     args = ap.parse_args()
+    if args.study == "batch":
+        steps = args.steps
+        batch_study(args.instances, steps, window=steps // 2, peak_gbs=args.peak,
+                    out_path=args.out)
+        return
     if args.study == "adjoint":
         steps = args.steps if args.steps != 20000 else 7000
         window = (steps - 2000, steps) if steps > 2000 else (steps // 2, steps)

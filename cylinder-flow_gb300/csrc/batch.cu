@@ -50,6 +50,7 @@ struct cflbm_batch {
   long long cells = 0;
   double bytes_per_cell = 0;
   cudaEvent_t done = nullptr;
+  cflbm::SweepFork fork{nullptr, nullptr, nullptr};  // solid-work kernel beside the fast one
   std::vector<double> tune_ms;  // timing of each candidate (for cflbm_batch_info)
 };
 
@@ -75,15 +76,22 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
   using E = typename SF::elem;
   __shared__ SweepArgs a;
   const int lane = threadIdx.x, wid = threadIdx.y, tid = wid * 32 + lane;
-  for (int w = blockIdx.x; w < n_work; w += gridDim.x) {
+  // Each block takes a contiguous range of work items (items are ordered by
+  // instance, then z, y, x), so the instance's arguments are staged in shared
+  // memory only when the range crosses into the next instance.
+  const int w0 = (int)((long long)blockIdx.x * n_work / gridDim.x);
+  const int w1 = (int)((long long)(blockIdx.x + 1) * n_work / gridDim.x);
+  int staged = -1;
+  for (int w = w0; w < w1; ++w) {
     const int4 wk = work[w];  // (instance, x tile, y tile | listed block, z)
-    __syncthreads();
-    {
+    if (wk.x != staged) {     // block-uniform
+      __syncthreads();
       const int *src = reinterpret_cast<const int *>(args + 4 * (long long)wk.x + sel);
       int *dst = reinterpret_cast<int *>(&a);
       for (int k = tid; k < (int)(sizeof(SweepArgs) / sizeof(int)); k += 32 * BY) dst[k] = src[k];
+      __syncthreads();
+      staged = wk.x;
     }
-    __syncthreads();
     const int nx = a.L.nx, ny = a.L.ny;
     int x, y, z;
     bool active;
@@ -225,11 +233,18 @@ cudaError_t launch_batch(const cflbm_batch *b, int by, int kind, int sel, int gr
   return launch_batch_st<27, F16Dev>(b, by, kind, sel, grid, s);
 }
 
-// One batch step: both launches, reading buffer `parity` of every instance.
+// One batch step: both launches, reading buffer `parity` of every instance.  The
+// solid-work kernel (tiles next to a body or on a wall row; latency-bound, with
+// the force reduction) runs on the higher-priority side stream beside the fast
+// kernel; the two write disjoint cells.
 int batch_one_step(cflbm_batch *b, int by, int grid, bool macros, bool swap) {
   const int sel = b->parity * 2 + (macros ? 1 : 0);
+  BCK(cudaEventRecord(b->fork.fork, b->stream));
+  BCK(cudaStreamWaitEvent(b->fork.side, b->fork.fork, 0));
+  BCK(launch_batch(b, by, 1, sel, grid, b->fork.side));
+  BCK(cudaEventRecord(b->fork.join, b->fork.side));
   BCK(launch_batch(b, by, 0, sel, grid, b->stream));
-  BCK(launch_batch(b, by, 1, sel, grid, b->stream));
+  BCK(cudaStreamWaitEvent(b->stream, b->fork.join, 0));
   if (swap) {
     b->parity ^= 1;
     ++b->steps_done;
@@ -249,6 +264,10 @@ void free_batch(cflbm_batch *b) {
     if (b->d_work_solid[k]) cudaFree(b->d_work_solid[k]);
   }
   if (b->done) cudaEventDestroy(b->done);
+  if (b->fork.side) cudaStreamSynchronize(b->fork.side);
+  if (b->fork.fork) cudaEventDestroy(b->fork.fork);
+  if (b->fork.join) cudaEventDestroy(b->fork.join);
+  if (b->fork.side) cudaStreamDestroy(b->fork.side);
   for (auto *h : b->inst) cflbm_destroy(h);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -300,6 +319,13 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
   BCK(cudaSetDevice(b->device));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   BCK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+  {
+    int lo = 0, hi = 0;
+    BCK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    BCK(cudaStreamCreateWithPriority(&b->fork.side, cudaStreamNonBlocking, hi));
+    BCK(cudaEventCreateWithFlags(&b->fork.fork, cudaEventDisableTiming));
+    BCK(cudaEventCreateWithFlags(&b->fork.join, cudaEventDisableTiming));
+  }
   int sms = 0;
   BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
   b->sms = sms;
@@ -416,7 +442,7 @@ int cflbm_batch_step(cflbm_batch *b, int nsteps) {
         return rc;
       }
       BCK(ec);
-      cudaError_t ei = cudaGraphInstantiate(&b->graph[par], g, 0);
+      cudaError_t ei = cudaGraphInstantiate(&b->graph[par], g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       BCK(ei);
       b->parity = par;  // capture walked the parity through an even number of steps
