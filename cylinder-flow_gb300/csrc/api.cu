@@ -554,9 +554,13 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   }
   sa.wall_y = h->cfg.wall_y;
   sa.wall_z = h->cfg.wall_z;
+  // Inlet populations in storage units (the FP16 format's power-of-two scale).
   for (int i = 0; i < h->Q; ++i) {
-    sa.f_in[i] = h->f_in[i];
-    sa.f_in_f[i] = (float)h->f_in[i];
+    const double sc = h->cfg.storage != CFLBM_STORE_FP16DEV
+                          ? 1.0
+                          : (h->Q == 27 ? (double)Lat<27>::h_scale(i) : (double)Lat<9>::h_scale(i));
+    sa.f_in[i] = h->f_in[i] * sc;
+    sa.f_in_f[i] = (float)(h->f_in[i] * sc);
   }
   sa.tile_slow = h->d_tile_slow;
   sa.slow_tiles = h->d_slow_tiles;

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
               f[I] = pull_resolved<Q, ST, A, I>(fa, c, S, x, y, z, links, a);
             },
             std::make_integer_sequence<int, Q>{});
-        if (valid && !solid_here) cell_force<Q, A>(f, links, Fxa, Fya, Fza);
+        if (valid && !solid_here) cell_force<Q, A, SF>(f, links, Fxa, Fya, Fza);
         Fx = f2d_bits(Fxa);
         Fy = f2d_bits(Fya);
         Fz = f2d_bits(Fza);
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
             std::make_integer_sequence<int, Q>{});
       }
       A rho3, ux, uy, uz;
-      moments<L, A>(f, rho3, ux, uy, uz);
+      moments<L, A, SF>(f, rho3, ux, uy, uz);
       if (solid_here) {
         rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
       }

@@ -125,8 +125,14 @@ __device__ __forceinline__ float d2f_bits(double d) {
   return __uint_as_float(t | (hi & 0x80000000u));
 }
 
+// Storage codecs.  load/store move values in "storage units": the population
+// times scale<L>(i) (1 for FP64 and FP32; the FP16 format's power of two), so
+// the FP16 path converts without a multiply; the sweep helpers fold 1/scale and
+// scale into their constants (moments, cell_force, bgk_relax, inlet values).
 template <> struct Store<double> {
   using elem = double;
+  template <class L>
+  __host__ __device__ static constexpr double scale(int) { return 1.0; }
   template <class A, class L>
   __device__ static A load(const elem *p, int) {
     if constexpr (sizeof(A) == 4) return d2f_bits(__ldg(p));
@@ -141,6 +147,8 @@ template <> struct Store<double> {
 
 template <> struct Store<float> {
   using elem = float;
+  template <class L>
+  __host__ __device__ static constexpr double scale(int) { return 1.0; }
   template <class A, class L>
   __device__ static A load(const elem *p, int) { return static_cast<A>(__ldg(p)); }
   template <class A, class L>
@@ -149,13 +157,15 @@ template <> struct Store<float> {
 
 template <> struct Store<F16Dev> {
   using elem = __half;
+  template <class L>
+  __host__ __device__ static constexpr double scale(int i) { return L::h_scale(i); }
   template <class A, class L>
-  __device__ static A load(const elem *p, int i) {
-    return static_cast<A>(__half2float(__ldg(p)) * (1.0f / L::h_scale(i)));
+  __device__ static A load(const elem *p, int) {
+    return static_cast<A>(__half2float(__ldg(p)));
   }
   template <class A, class L>
-  __device__ static void store(elem *p, A v, int i) {
-    *p = __float2half_rn(static_cast<float>(v) * L::h_scale(i));
+  __device__ static void store(elem *p, A v, int) {
+    *p = __float2half_rn(static_cast<float>(v));
   }
 };
 #endif  // __CUDACC__

@@ -34,12 +34,14 @@ namespace cflbm {
 
 // BGK relaxation toward the incompressible equilibrium, written per +/- pair:
 // the pair shares (e.u)^2 and the even part of feq; the odd part flips sign.
-template <class L, class A>
+// f is in storage units (SF::scale): the weights carry the scale, which a pair
+// shares (opposite directions have the same weight).
+template <class L, class A, class SF>
 __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const SweepArgs &a) {
   A om;
   if constexpr (sizeof(A) == 8) om = a.omega; else om = a.omega_f;
   const A c0 = rho3 - A(1.5) * (ux * ux + uy * uy + uz * uz);
-  f[0] = f[0] + om * (A(L::w(0)) * c0 - f[0]);
+  f[0] = f[0] + om * (A(L::w(0) * SF::template scale<L>(0)) * c0 - f[0]);
 #pragma unroll
   for (int k = 0; k < L::NPAIR; ++k) {
     const int i = L::pair(k), j = L::opp(L::pair(k));
@@ -47,29 +49,31 @@ __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const 
     if (L::ex(i) > 0) eu += ux; else if (L::ex(i) < 0) eu -= ux;
     if (L::ey(i) > 0) eu += uy; else if (L::ey(i) < 0) eu -= uy;
     if (L::ez(i) > 0) eu += uz; else if (L::ez(i) < 0) eu -= uz;
-    const A sym = A(L::w(i)) * (c0 + A(4.5) * eu * eu);
-    const A asym = A(3.0 * L::w(i)) * eu;
+    const A sym = A(L::w(i) * SF::template scale<L>(i)) * (c0 + A(4.5) * eu * eu);
+    const A asym = A(3.0 * L::w(i) * SF::template scale<L>(i)) * eu;
     f[i] = f[i] + om * ((sym + asym) - f[i]);
     f[j] = f[j] + om * ((sym - asym) - f[j]);
   }
 }
 
-// Moments in deviation form: rho3 = 3p = sum f, u = sum f e.
-template <class L, class A>
+// Moments in deviation form: rho3 = 3p = sum f, u = sum f e, from populations
+// in storage units (the 1/scale factors are exact powers of two, 1 for FP32/64).
+template <class L, class A, class SF>
 __device__ __forceinline__ void moments(const A *f, A &rho3, A &ux, A &uy, A &uz) {
-  rho3 = f[0];
+  rho3 = f[0] * A(1.0 / SF::template scale<L>(0));
   ux = A(0);
   uy = A(0);
   uz = A(0);
 #pragma unroll
   for (int k = 0; k < L::NPAIR; ++k) {
     const int i = L::pair(k), j = L::opp(L::pair(k));
+    const A inv = A(1.0 / SF::template scale<L>(i));
     const A s = f[i] + f[j];
     const A d = f[i] - f[j];
-    rho3 += s;
-    if (L::ex(i) > 0) ux += d; else if (L::ex(i) < 0) ux -= d;
-    if (L::ey(i) > 0) uy += d; else if (L::ey(i) < 0) uy -= d;
-    if (L::ez(i) > 0) uz += d; else if (L::ez(i) < 0) uz -= d;
+    rho3 += s * inv;
+    if (L::ex(i) > 0) ux += d * inv; else if (L::ex(i) < 0) ux -= d * inv;
+    if (L::ey(i) > 0) uy += d * inv; else if (L::ey(i) < 0) uy -= d * inv;
+    if (L::ez(i) > 0) uz += d * inv; else if (L::ez(i) < 0) uz -= d * inv;
   }
 }
 
@@ -98,7 +102,7 @@ __device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long
     uy *= s;
     uz *= s;
   }
-  bgk_relax<L, A>(f, rho3, ux, uy, uz, a);
+  bgk_relax<L, A, SF>(f, rho3, ux, uy, uz, a);
   if (store) {
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) SF::template store<A, L>(fb + i * S + c, f[i], i);
@@ -126,7 +130,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_kernel(const 
     f[i] = SF::template load<A, L>(fa + i * S + c - a.L.off(L::ex(i), L::ey(i), L::ez(i)), i);
 
   A rho3, ux, uy, uz;
-  moments<L, A>(f, rho3, ux, uy, uz);
+  moments<L, A, SF>(f, rho3, ux, uy, uz);
   const long long cell = ((long long)z * a.L.ny + y) * a.L.nx + x;
   if (mask_solid(a.mask, a.nxw, a.L.ny, x, y, z)) {
     rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
@@ -167,7 +171,7 @@ __device__ __forceinline__ void static_for(F &&f, std::integer_sequence<int, Is.
 }
 
 // Inlet equilibrium population in the arithmetic type (no FP64 conversion in
-// FP32 sweeps).
+// FP32 sweeps), in storage units (the host scales f_in / f_in_f).
 template <class A>
 __device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
   if constexpr (sizeof(A) == 8) return a.f_in[i]; else return a.f_in_f[i];
@@ -240,14 +244,16 @@ __device__ __forceinline__ A pull_resolved(const typename Store<ST>::elem *__res
 }
 
 // Force of one cell's solid bounce-backs, summed in the arithmetic type (at most
-// Q - 1 terms): each adds 2 f*_{opp(I)}(X) e_{opp(I)} = -2 v_I e_I.
-template <int Q, class A>
+// Q - 1 terms): each adds 2 f*_{opp(I)}(X) e_{opp(I)} = -2 v_I e_I (v_I in
+// storage units, scale of I).
+template <int Q, class A, class SF>
 __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A &fy, A &fz) {
   static_for(
       [&](auto ic) {
         constexpr int I = decltype(ic)::value;
         if constexpr (I > 0) {
-          const A m = ((links >> I) & 1u) ? A(2) * f[I] : A(0);
+          const A m = ((links >> I) & 1u)
+                          ? A(2.0 / SF::template scale<Lat<Q>>(I)) * f[I] : A(0);
           if constexpr (Lat<Q>::ex(I) != 0) fx -= Lat<Q>::ex(I) * m;
           if constexpr (Lat<Q>::ey(I) != 0) fy -= Lat<Q>::ey(I) * m;
           if constexpr (Lat<Q>::ez(I) != 0) fz -= Lat<Q>::ez(I) * m;
@@ -307,7 +313,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
             f[I] = pull_resolved<Q, ST, A, I>(fa, c, S, x, y, z, links, a);
           },
           std::make_integer_sequence<int, Q>{});
-      if (valid && !solid_here) cell_force<Q, A>(f, links, Fx, Fy, Fz);
+      if (valid && !solid_here) cell_force<Q, A, SF>(f, links, Fx, Fy, Fz);
     } else {
       static_for(
           [&](auto ic) {
@@ -317,7 +323,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
           std::make_integer_sequence<int, Q>{});
     }
     A rho3, ux, uy, uz;
-    moments<L, A>(f, rho3, ux, uy, uz);
+    moments<L, A, SF>(f, rho3, ux, uy, uz);
     if (solid_here) {
       rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
     }
