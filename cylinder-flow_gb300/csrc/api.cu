@@ -352,7 +352,10 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   L.G = G;
   L.Gz = d3 ? G : 0;
   L.xoff = align;
-  L.px = ((align + nx + G + 4 + align - 1) / align) * align;
+  // Row pitch: room for whole 32-cell warp tiles past the last interior cell, so
+  // no lane of a partial last tile reads into the next row.
+  const int nx_tiles = ((nx + 31) / 32) * 32;
+  L.px = ((align + nx_tiles + G + 4 + align - 1) / align) * align;
   L.nyp = ny + 2 * G;
   L.nzp = nz + 2 * L.Gz;
   if (cfg->layout == CFLBM_LAYOUT_ROWS) {

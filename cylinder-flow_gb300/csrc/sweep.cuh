@@ -27,54 +27,130 @@
 //                            boundary code out of the first launch holds it at
 //                            64 registers with all loads independent.
 #pragma once
+#include <type_traits>
 #include <utility>
 #include "solver.cuh"
 
 namespace cflbm {
 
+template <class F, int... Is>
+__device__ __forceinline__ void static_for(F &&f, std::integer_sequence<int, Is...>) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+
+// Collision arithmetic over V = float, double or float2 (two cells per thread,
+// GB300's packed FFMA2/FADD2/FMUL2).  Every operation is explicitly rounded, so
+// the compiler neither contracts nor reorders: a cell gets the same bits from
+// every kernel that collides it, scalar or packed.
+template <class V> struct VA;
+template <> struct VA<float> {
+  using S = float;
+  __device__ static float splat(float s) { return s; }
+  __device__ static float add(float a, float b) { return __fadd_rn(a, b); }
+  __device__ static float sub(float a, float b) { return __fsub_rn(a, b); }
+  __device__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+  __device__ static float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+};
+template <> struct VA<double> {
+  using S = double;
+  __device__ static double splat(double s) { return s; }
+  __device__ static double add(double a, double b) { return __dadd_rn(a, b); }
+  __device__ static double sub(double a, double b) { return __dsub_rn(a, b); }
+  __device__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+  __device__ static double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+};
+template <> struct VA<float2> {
+  using S = float;
+  __device__ static float2 splat(float s) { return make_float2(s, s); }
+  __device__ static float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+  // a - b = fma(b, -1, a): the product is exact, so one rounding as in FADD.
+  __device__ static float2 sub(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+  }
+  __device__ static float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+  __device__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+};
+
+// acc + K v with K = NUM / DEN a power of two (1 and -1 without a product).
+template <class V, int NUM, int DEN>
+__device__ __forceinline__ V acc_(V acc, V v) {
+  using O = VA<V>;
+  if constexpr (NUM == DEN) return O::add(acc, v);
+  else if constexpr (NUM == -DEN) return O::sub(acc, v);
+  else return O::fma(v, O::splat(typename O::S(double(NUM) / double(DEN))), acc);
+}
+
 // BGK relaxation toward the incompressible equilibrium, written per +/- pair:
 // the pair shares (e.u)^2 and the even part of feq; the odd part flips sign.
 // f is in storage units (SF::scale): the weights carry the scale, which a pair
 // shares (opposite directions have the same weight).
+//   c0 = rho3 - 1.5 |u|^2
+//   feq_{i,j} = ws_i (c0 + 4.5 (e.u)^2) +- 3 ws_i (e.u),  ws_i = w_i scale_i
+//   f <- f + omega (feq - f)
+template <class L, class V, class SF>
+__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, V om) {
+  using O = VA<V>;
+  using S = typename O::S;
+  const V usq = O::fma(ux, ux, O::fma(uy, uy, O::mul(uz, uz)));
+  const V c0 = O::fma(O::splat(S(-1.5)), usq, rho3);
+  f[0] = O::fma(om, O::sub(O::mul(O::splat(S(L::w(0) * SF::template scale<L>(0))), c0), f[0]),
+                f[0]);
+  static_for(
+      [&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int i = L::pair(k), j = L::opp(L::pair(k));
+        constexpr double ws = L::w(i) * SF::template scale<L>(i);
+        constexpr int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+        // e.u with the components in x, y, z order
+        V eu;
+        if constexpr (ex != 0) {
+          eu = ex > 0 ? ux : O::sub(O::splat(S(0)), ux);
+          if constexpr (ey != 0) eu = ey > 0 ? O::add(eu, uy) : O::sub(eu, uy);
+          if constexpr (ez != 0) eu = ez > 0 ? O::add(eu, uz) : O::sub(eu, uz);
+        } else if constexpr (ey != 0) {
+          eu = ey > 0 ? uy : O::sub(O::splat(S(0)), uy);
+          if constexpr (ez != 0) eu = ez > 0 ? O::add(eu, uz) : O::sub(eu, uz);
+        } else {
+          eu = ez > 0 ? uz : O::sub(O::splat(S(0)), uz);
+        }
+        const V sym = O::mul(O::splat(S(ws)), O::fma(O::splat(S(4.5)), O::mul(eu, eu), c0));
+        const V asym = O::mul(O::splat(S(3.0 * ws)), eu);
+        f[i] = O::fma(om, O::sub(O::add(sym, asym), f[i]), f[i]);
+        f[j] = O::fma(om, O::sub(O::sub(sym, asym), f[j]), f[j]);
+      },
+      std::make_integer_sequence<int, L::NPAIR>{});
+}
+
 template <class L, class A, class SF>
 __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const SweepArgs &a) {
   A om;
   if constexpr (sizeof(A) == 8) om = a.omega; else om = a.omega_f;
-  const A c0 = rho3 - A(1.5) * (ux * ux + uy * uy + uz * uz);
-  f[0] = f[0] + om * (A(L::w(0) * SF::template scale<L>(0)) * c0 - f[0]);
-#pragma unroll
-  for (int k = 0; k < L::NPAIR; ++k) {
-    const int i = L::pair(k), j = L::opp(L::pair(k));
-    A eu = A(0);
-    if (L::ex(i) > 0) eu += ux; else if (L::ex(i) < 0) eu -= ux;
-    if (L::ey(i) > 0) eu += uy; else if (L::ey(i) < 0) eu -= uy;
-    if (L::ez(i) > 0) eu += uz; else if (L::ez(i) < 0) eu -= uz;
-    const A sym = A(L::w(i) * SF::template scale<L>(i)) * (c0 + A(4.5) * eu * eu);
-    const A asym = A(3.0 * L::w(i) * SF::template scale<L>(i)) * eu;
-    f[i] = f[i] + om * ((sym + asym) - f[i]);
-    f[j] = f[j] + om * ((sym - asym) - f[j]);
-  }
+  bgk_relax_v<L, A, SF>(f, rho3, ux, uy, uz, om);
 }
 
 // Moments in deviation form: rho3 = 3p = sum f, u = sum f e, from populations
 // in storage units (the 1/scale factors are exact powers of two, 1 for FP32/64).
-template <class L, class A, class SF>
-__device__ __forceinline__ void moments(const A *f, A &rho3, A &ux, A &uy, A &uz) {
-  rho3 = f[0] * A(1.0 / SF::template scale<L>(0));
-  ux = A(0);
-  uy = A(0);
-  uz = A(0);
-#pragma unroll
-  for (int k = 0; k < L::NPAIR; ++k) {
-    const int i = L::pair(k), j = L::opp(L::pair(k));
-    const A inv = A(1.0 / SF::template scale<L>(i));
-    const A s = f[i] + f[j];
-    const A d = f[i] - f[j];
-    rho3 += s * inv;
-    if (L::ex(i) > 0) ux += d * inv; else if (L::ex(i) < 0) ux -= d * inv;
-    if (L::ey(i) > 0) uy += d * inv; else if (L::ey(i) < 0) uy -= d * inv;
-    if (L::ez(i) > 0) uz += d * inv; else if (L::ez(i) < 0) uz -= d * inv;
-  }
+template <class L, class V, class SF>
+__device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
+  using O = VA<V>;
+  using S = typename O::S;
+  constexpr int S0 = (int)SF::template scale<L>(0);
+  if constexpr (S0 == 1) rho3 = f[0];
+  else rho3 = O::mul(f[0], O::splat(S(1.0 / S0)));
+  ux = uy = uz = O::splat(S(0));
+  static_for(
+      [&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int i = L::pair(k), j = L::opp(L::pair(k));
+        constexpr int SC = (int)SF::template scale<L>(i);
+        const V sm = O::add(f[i], f[j]);
+        const V d = O::sub(f[i], f[j]);
+        rho3 = acc_<V, 1, SC>(rho3, sm);
+        if constexpr (L::ex(i) != 0) ux = acc_<V, L::ex(i), SC>(ux, d);
+        if constexpr (L::ey(i) != 0) uy = acc_<V, L::ey(i), SC>(uy, d);
+        if constexpr (L::ez(i) != 0) uz = acc_<V, L::ez(i), SC>(uz, d);
+      },
+      std::make_integer_sequence<int, L::NPAIR>{});
 }
 
 // Macros out (when requested), Brinkman damping of the equilibrium velocity,
@@ -88,19 +164,19 @@ __device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long
       a.mu[cell] = f2d_bits(ux);
       a.mv[cell] = f2d_bits(uy);
       a.mw[cell] = f2d_bits(uz);
-      a.mp[cell] = f2d_bits(rho3 * (1.0f / 3.0f));
+      a.mp[cell] = f2d_bits(__fmul_rn(rho3, 1.0f / 3.0f));
     } else {
       a.mu[cell] = ux;
       a.mv[cell] = uy;
       a.mw[cell] = uz;
-      a.mp[cell] = rho3 / 3.0;
+      a.mp[cell] = __ddiv_rn(rho3, 3.0);
     }
   }
   if (a.alpha) {
-    const A s = A(1) - static_cast<A>(a.alpha[cell]);
-    ux *= s;
-    uy *= s;
-    uz *= s;
+    const A s = VA<A>::sub(A(1), static_cast<A>(a.alpha[cell]));
+    ux = VA<A>::mul(ux, s);
+    uy = VA<A>::mul(uy, s);
+    uz = VA<A>::mul(uz, s);
   }
   bgk_relax<L, A, SF>(f, rho3, ux, uy, uz, a);
   if (store) {
@@ -165,10 +241,6 @@ template <int Q, int I> struct DirC {
   static constexpr int myz = mirror<L>(mirror<L>(I, 1), 2);
 };
 
-template <class F, int... Is>
-__device__ __forceinline__ void static_for(F &&f, std::integer_sequence<int, Is...>) {
-  (f(std::integral_constant<int, Is>{}), ...);
-}
 
 // Inlet equilibrium population in the arithmetic type (no FP64 conversion in
 // FP32 sweeps), in storage units (the host scales f_in / f_in_f).
@@ -252,14 +324,108 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
       [&](auto ic) {
         constexpr int I = decltype(ic)::value;
         if constexpr (I > 0) {
+          using O = VA<A>;
           const A m = ((links >> I) & 1u)
-                          ? A(2.0 / SF::template scale<Lat<Q>>(I)) * f[I] : A(0);
-          if constexpr (Lat<Q>::ex(I) != 0) fx -= Lat<Q>::ex(I) * m;
-          if constexpr (Lat<Q>::ey(I) != 0) fy -= Lat<Q>::ey(I) * m;
-          if constexpr (Lat<Q>::ez(I) != 0) fz -= Lat<Q>::ez(I) * m;
+                          ? O::mul(A(2.0 / SF::template scale<Lat<Q>>(I)), f[I]) : A(0);
+          if constexpr (Lat<Q>::ex(I) != 0) fx = Lat<Q>::ex(I) > 0 ? O::sub(fx, m) : O::add(fx, m);
+          if constexpr (Lat<Q>::ey(I) != 0) fy = Lat<Q>::ey(I) > 0 ? O::sub(fy, m) : O::add(fy, m);
+          if constexpr (Lat<Q>::ez(I) != 0) fz = Lat<Q>::ez(I) > 0 ? O::sub(fz, m) : O::add(fz, m);
         }
       },
       std::make_integer_sequence<int, Q>{});
+}
+
+// Interior channel sweep with two cells per thread and packed FP32x2
+// arithmetic: a warp takes the two warp tiles 2b and 2b + 1 of a row, so a thread
+// owns cells x and x + 32, whose loads and stores share their address (the
+// second is an immediate 32 elements further).  Moments and BGK run once on
+// float2 values (FADD2/FMUL2/FFMA2), halving the arithmetic instructions of
+// the issue-bound FP32-collision forms.  Listed tiles are skipped per half.
+template <int Q, class ST, int I>
+__device__ __forceinline__ float2 pull_pair(const typename Store<ST>::elem *__restrict__ p,
+                                           const typename Store<ST>::elem *__restrict__ pm0,
+                                           const typename Store<ST>::elem *__restrict__ pm1,
+                                           long long S, long long rs, long long zs, bool act0,
+                                           bool act1, bool inlet0, const SweepArgs &a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using Dd = DirC<Q, I>;
+  const long long off = I * S - (Dd::ex + Dd::ey * rs + Dd::ez * zs);
+  float v0 = 0.0f, v1 = 0.0f;
+  if constexpr (Dd::ex < 0) {  // the outlet column repeats itself (pm = p - 1 there)
+    if (act0) v0 = SF::template load<float, L>(pm0 + off, I);
+    if (act1) v1 = SF::template load<float, L>(pm1 + off, I);
+  } else {
+    if (act0) v0 = SF::template load<float, L>(p + off, I);
+    if (act1) v1 = SF::template load<float, L>(p + off + 32, I);
+  }
+  if constexpr (Dd::ex > 0) v0 = inlet0 ? a.f_in_f[I] : v0;
+  return make_float2(v0, v1);
+}
+
+template <int Q, class ST, int MINB>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
+    sweep_channel2_kernel(const SweepArgs a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  using O = VA<float2>;
+  const int nx = a.L.nx, ny = a.L.ny;
+  const int lane = threadIdx.x;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y, z = blockIdx.z;
+  if (y >= ny) return;
+  const int w0 = 2 * blockIdx.x;
+  const long long trow = ((long long)z * ny + y) * a.nxw;
+  const bool act0 = !a.tile_slow[trow + w0];
+  const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
+  if (!act0 && !act1) return;  // whole warp
+  const int x0 = 32 * w0 + lane, x1 = x0 + 32;
+  const bool st0 = act0 && x0 < nx, st1 = act1 && x1 < nx;
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x0, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  const E *__restrict__ p = fa + c;
+  const E *__restrict__ pm0 = p - (x0 == nx - 1 ? 1 : 0);
+  const E *__restrict__ pm1 = p + 32 - (x1 == nx - 1 ? 1 : 0);
+  const bool inlet0 = x0 == 0;
+  float2 f[Q];
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        f[I] = pull_pair<Q, ST, I>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1, inlet0, a);
+      },
+      std::make_integer_sequence<int, Q>{});
+  float2 rho3, ux, uy, uz;
+  moments<L, float2, SF>(f, rho3, ux, uy, uz);
+  const long long cell0 = ((long long)z * ny + y) * nx + x0;
+  if (a.mu) {
+    if (st0) {
+      a.mu[cell0] = f2d_bits(ux.x);
+      a.mv[cell0] = f2d_bits(uy.x);
+      a.mw[cell0] = f2d_bits(uz.x);
+      a.mp[cell0] = f2d_bits(__fmul_rn(rho3.x, 1.0f / 3.0f));
+    }
+    if (st1) {
+      a.mu[cell0 + 32] = f2d_bits(ux.y);
+      a.mv[cell0 + 32] = f2d_bits(uy.y);
+      a.mw[cell0 + 32] = f2d_bits(uz.y);
+      a.mp[cell0 + 32] = f2d_bits(__fmul_rn(rho3.y, 1.0f / 3.0f));
+    }
+  }
+  if (a.alpha) {
+    const float2 sb = make_float2(__fsub_rn(1.0f, st0 ? a.alpha[cell0] : 0.0f),
+                                  __fsub_rn(1.0f, st1 ? a.alpha[cell0 + 32] : 0.0f));
+    ux = O::mul(ux, sb);
+    uy = O::mul(uy, sb);
+    uz = O::mul(uz, sb);
+  }
+  bgk_relax_v<L, float2, SF>(f, rho3, ux, uy, uz, O::splat(a.omega_f));
+  E *__restrict__ q = static_cast<E *>(a.fb) + c;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    if (st0) SF::template store<float, L>(q + i * S, f[i].x, i);
+    if (st1) SF::template store<float, L>(q + i * S + 32, f[i].y, i);
+  }
 }
 
 // Channel sweep.  BOUNDARY = false: every warp tile that is not listed (rows
@@ -404,6 +570,18 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
   }
 }
 
+// The interior launch: FP32 collision on FP32 or FP16 storage takes the packed
+// two-cells-per-thread kernel; the others the one-cell kernel.
+template <int Q, class ST, class A, int MINB_FAST>
+void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) {
+  if constexpr (sizeof(A) == 4 && !std::is_same<ST, double>::value) {
+    dim3 g2((a.nxw + 1) / 2, grid.y, grid.z);
+    sweep_channel2_kernel<Q, ST, 4><<<g2, block, 0, s>>>(a);
+  } else {
+    sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+  }
+}
+
 template <int Q, class ST, class A, int MINB_FAST, int MINB_SLOW>
 cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const SweepFork *fk) {
   dim3 block(SWEEP_BX, SWEEP_BY, 1);
@@ -418,11 +596,11 @@ cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const Swe
     sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, fk->side>>>(a);
     e = cudaEventRecord(fk->join, fk->side);
     if (e != cudaSuccess) return e;
-    sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+    launch_interior<Q, ST, A, MINB_FAST>(a, grid, block, s);
     e = cudaStreamWaitEvent(s, fk->join, 0);
     if (e != cudaSuccess) return e;
   } else {
-    sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+    launch_interior<Q, ST, A, MINB_FAST>(a, grid, block, s);
     sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
   }
   count_launch(2);
