@@ -328,6 +328,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaSetDevice(cfg->device));
   CK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   CK_CUDA(cudaEventCreateWithFlags(&h->ev_sync, cudaEventDisableTiming));
+  CK_CUDA(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, cfg->device));
   if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
     // Side stream of the channel sweep's listed-tile kernel, at the highest
     // priority so its blocks are scheduled ahead of the interior kernel's.
@@ -565,6 +566,8 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
     sa.f_in[i] = h->f_in[i] * sc;
     sa.f_in_f[i] = (float)(h->f_in[i] * sc);
   }
+  sa.bnd_blocks = (int)std::max<long long>(
+      1, std::min<long long>((h->n_slow + SWEEP_BY - 1) / SWEEP_BY, h->sms));
   sa.tile_slow = h->d_tile_slow;
   sa.slow_tiles = h->d_slow_tiles;
   sa.links_bits = h->d_links_bits;

@@ -14,6 +14,7 @@ struct cflbm_handle {
   int nxw = 0;
   int esize = 8;
   cudaStream_t stream = nullptr;
+  int sms = 1;  // multiprocessors of the device
   cflbm::SweepFork fork{nullptr, nullptr, nullptr};  // channel sweep: side stream + events
   void *fA = nullptr, *fB = nullptr;
   size_t f_bytes = 0;

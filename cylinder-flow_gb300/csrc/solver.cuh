@@ -75,6 +75,7 @@ struct SweepArgs {
   double *hist;          // force history, 3 doubles per step
   long long *step;       // device step counter (history slot = step % cap)
   long long cap;
+  int bnd_blocks;        // grid of the listed-tile launch (persistent, about one block per SM)
 };
 
 struct FillArgs {

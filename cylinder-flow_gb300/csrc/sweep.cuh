@@ -442,26 +442,8 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
   using E = typename SF::elem;
   const int nx = a.L.nx, ny = a.L.ny;
   const int lane = threadIdx.x, wid = threadIdx.y;
-  int x, y, z;
-  bool active;
-  long long t = 0;
-  if constexpr (BOUNDARY) {
-    t = (long long)blockIdx.x * SWEEP_BY + wid;
-    active = t < a.n_slow;
-    const int tile = active ? a.slow_tiles[t] : 0;
-    const int row = tile / a.nxw;
-    y = row % ny;
-    z = row / ny;
-    x = (tile % a.nxw) * SWEEP_BX + lane;
-  } else {
-    y = blockIdx.y * SWEEP_BY + wid;
-    z = blockIdx.z;
-    x = blockIdx.x * SWEEP_BX + lane;
-    active = y < ny && !a.tile_slow[((long long)z * ny + (y < ny ? y : 0)) * a.nxw + blockIdx.x];
-    if (!active) return;  // whole warp
-  }
-  A Fx = A(0), Fy = A(0), Fz = A(0);
-  if (active) {  // warp-uniform
+  // One cell: pull, moments, (boundary: solid mask and force), relax, store.
+  auto cell_step = [&](int x, int y, int z, long long t, A &Fx, A &Fy, A &Fz) {
     const bool valid = x < nx;
     if (!valid) x = nx - 1;
     const long long S = a.L.S;
@@ -495,20 +477,40 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
     }
     const long long cell = ((long long)z * ny + y) * nx + x;
     finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
+  };
+  // Boundary launch: a small persistent grid (about one block per SM, so it
+  // leaves most of every SM to the interior launch running beside it) strides
+  // over the listed tiles; each thread carries its force sums in FP64.
+  double dx = 0.0, dy = 0.0, dz = 0.0;
+  if constexpr (BOUNDARY) {
+    for (long long base = (long long)blockIdx.x * SWEEP_BY; base < a.n_slow;
+         base += (long long)gridDim.x * SWEEP_BY) {
+      const long long t = base + wid;
+      if (t >= a.n_slow) continue;  // warp-uniform
+      const int tile = a.slow_tiles[t];
+      const int row = tile / a.nxw;
+      A Fx = A(0), Fy = A(0), Fz = A(0);
+      cell_step((tile % a.nxw) * SWEEP_BX + lane, row % ny, row / ny, t, Fx, Fy, Fz);
+      if constexpr (sizeof(A) == 4) {
+        dx += f2d_bits(Fx);
+        dy += f2d_bits(Fy);
+        dz += f2d_bits(Fz);
+      } else {
+        dx += Fx;
+        dy += Fy;
+        dz += Fz;
+      }
+    }
+  } else {
+    const int y = blockIdx.y * SWEEP_BY + wid;
+    const int z = blockIdx.z;
+    if (y >= ny || a.tile_slow[((long long)z * ny + y) * a.nxw + blockIdx.x]) return;  // whole warp
+    A Fx = A(0), Fy = A(0), Fz = A(0);
+    cell_step(blockIdx.x * SWEEP_BX + lane, y, z, 0, Fx, Fy, Fz);
   }
   if constexpr (BOUNDARY) {
-    // Per-thread FP32/FP64 partials -> FP64; block partial -> partials[blockIdx.x];
-    // the last block sums all partials.
-    double dx, dy, dz;
-    if constexpr (sizeof(A) == 4) {
-      dx = f2d_bits(Fx);
-      dy = f2d_bits(Fy);
-      dz = f2d_bits(Fz);
-    } else {
-      dx = Fx;
-      dy = Fy;
-      dz = Fz;
-    }
+    // Per-thread FP64 sums; block partial -> partials[blockIdx.x]; the last
+    // block sums all partials in block order.
     constexpr int NW = SWEEP_BY;
     const int tid = wid * SWEEP_BX + lane;
     __shared__ double sh[3][NW];
@@ -586,7 +588,7 @@ template <int Q, class ST, class A, int MINB_FAST, int MINB_SLOW>
 cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const SweepFork *fk) {
   dim3 block(SWEEP_BX, SWEEP_BY, 1);
   dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
-  const int sb = (a.n_slow + SWEEP_BY - 1) / SWEEP_BY;
+  const int sb = a.bnd_blocks;
   if (fk && fk->side) {
     // The listed tiles go first on the (higher-priority) side stream, so their
     // latency-bound blocks overlap the interior kernel's streaming.
