@@ -577,10 +577,10 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
 template <int Q, class ST, class A, int MINB_FAST>
 void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) {
   if constexpr (sizeof(A) == 4 && !std::is_same<ST, double>::value) {
-    // Blocks per SM: as many as fit without spills (80 registers for FP32
-    // storage, 96 for FP16, whose codec adds a few), measured on the D3Q27 bench
-    // step: FP32 0.850 / 0.908 / 0.937 of the copy peak at 4 / 5 / 6 per SM,
-    // FP16 0.613 / 0.636 / 0.632.
+    // Blocks per SM, measured on the D3Q27 bench step: FP32 storage 0.850 /
+    // 0.908 / 0.937 of the copy peak at 4 / 5 / 6 per SM (80 registers, no
+    // spills at 6; 7 and 8 spill); FP16 0.613 / 0.636 / 0.632 (96 registers
+    // and a 44-byte spill at 5).
     constexpr int M2 = std::is_same<ST, float>::value ? 6 : 5;
     dim3 g2((a.nxw + 1) / 2, grid.y, grid.z);
     sweep_channel2_kernel<Q, ST, M2><<<g2, block, 0, s>>>(a);
