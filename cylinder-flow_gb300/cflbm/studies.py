@@ -37,6 +37,18 @@ import numpy as np
 from . import analysis
 from .solver import Solver
 
+def measured_peak_gbs() -> float:
+    """HBM copy peak of this pool (MEASURED_PEAKS.json at the repository root),
+    else the 6800 GB/s fallback of an earlier GB300 measurement."""
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__)))), "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    return 6800.0
+
+
 FORMS = [  # name, storage, compute
     ("fp64_arith", "fp64", "fp64"),
     ("fp64_store", "fp64", "fp32"),
@@ -216,9 +228,11 @@ def batch_cases(n=64, seed=2025, u0=0.05):
     return out
 
 
-def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=6656.0,
+def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=None,
                 out_path=None, sequential=True):
     from .solver import Batch
+    if peak_gbs is None:
+        peak_gbs = measured_peak_gbs()
     cases = batch_cases(n)
     cfgs = [{k: v for k, v in c.items() if k != "re"} for c in cases]
     cells = sum(c["nx"] * c["ny"] for c in cfgs)
@@ -287,7 +301,8 @@ def main():
     ap.add_argument("--nz", type=int, default=384)
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--window", type=int, default=5000)
-    ap.add_argument("--peak", type=float, default=6656.0)
+    ap.add_argument("--peak", type=float, default=None,
+                    help="HBM peak in GB/s (default: MEASURED_PEAKS.json)")
     ap.add_argument("--out", default=None)
     ap.add_argument("--forms", default=",".join(f[0] for f in FORMS))
     ap.add_argument("--directions", type=int, default=16)
@@ -296,6 +311,8 @@ def main():
     ap.add_argument("--no-fd", action="store_true")
     ap.add_argument("--instances", type=int, default=64)
     args = ap.parse_args()
+    if args.peak is None:
+        args.peak = measured_peak_gbs()
     if args.study == "batch":
         steps = args.steps
         batch_study(args.instances, steps, window=steps // 2, peak_gbs=args.peak,
