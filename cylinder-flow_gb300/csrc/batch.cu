@@ -67,8 +67,11 @@ int bfail(int code, const std::string &msg) { return record_error(code, msg.c_st
       return bfail(CFLBM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
   } while (0)
 
+// Fast items (unlisted tiles) run two cells per thread with packed FP32x2
+// arithmetic (channel2_cells: cells x and x + 32 of a row, items 64 cells wide);
+// solid items (tiles next to a body or on a wall row) one cell per thread.
 template <int Q, class ST, class A, int BY, bool SOLID>
-__global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
+__global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
     batch_sweep_kernel(const SweepArgs *__restrict__ args, const int4 *__restrict__ work,
                        int n_work, int sel) {
   using L = Lat<Q>;
@@ -93,8 +96,8 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
       staged = wk.x;
     }
     const int nx = a.L.nx, ny = a.L.ny;
-    int x, y, z;
-    bool active;
+    int x = 0, y = 0, z = 0;
+    bool active = false;
     long long t = 0;
     if constexpr (SOLID) {
       t = (long long)wk.z * BY + wid;
@@ -107,8 +110,14 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 32 / BY)
     } else {
       y = wk.z * BY + wid;
       z = wk.w;
-      x = wk.y * 32 + lane;
-      active = y < ny && !a.tile_slow[((long long)z * ny + (y < ny ? y : 0)) * a.nxw + wk.y];
+      const int w0 = 2 * wk.y;
+      if (y < ny) {  // warp-uniform
+        const long long trow = ((long long)z * ny + y) * a.nxw;
+        const bool act0 = !a.tile_slow[trow + w0];
+        const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
+        if (act0 || act1) channel2_cells<Q, ST>(a, 32 * w0 + lane, y, z, act0, act1);
+      }
+      continue;
     }
     double Fx = 0.0, Fy = 0.0, Fz = 0.0;
     if (active) {  // warp-uniform
@@ -356,7 +365,7 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
     std::vector<int4> wf, ws;
     for (int k = 0; k < n; ++k) {
       const cflbm_handle *h = b->inst[k];
-      const int gx = (h->L.nx + 31) / 32, gy = (h->L.ny + by - 1) / by;
+      const int gx = (h->nxw + 1) / 2, gy = (h->L.ny + by - 1) / by;  // 64-cell items
       for (int z = 0; z < h->L.nz; ++z)
         for (int yb = 0; yb < gy; ++yb)
           for (int xb = 0; xb < gx; ++xb) wf.push_back(make_int4(k, xb, yb, z));
@@ -381,7 +390,7 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
     BCK(cudaEventCreate(&e1));
     float best = 1e30f;
     for (int ci = 0; ci < 4; ++ci)
-      for (int bps : {2, 4, 8, 16}) {
+      for (int bps : {2, 3, 4, 6, 8, 12, 16}) {
         const int by = BY_CANDIDATES[ci];
         if (32 * by * bps > 2048) continue;
         const int grid = bps * sms;

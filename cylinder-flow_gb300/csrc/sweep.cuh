@@ -363,23 +363,17 @@ __device__ __forceinline__ float2 pull_pair(const typename Store<ST>::elem *__re
   return make_float2(v0, v1);
 }
 
-template <int Q, class ST, int MINB>
-__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
-    sweep_channel2_kernel(const SweepArgs a) {
+// Cells x0 and x0 + 32 of row (y, z) (x0 = 32 * even warp tile + lane); act0 /
+// act1: the two warp tiles are unlisted (warp-uniform).
+template <int Q, class ST>
+__device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y, int z,
+                                               bool act0, bool act1) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
   using O = VA<float2>;
   const int nx = a.L.nx, ny = a.L.ny;
-  const int lane = threadIdx.x;
-  const int y = blockIdx.y * SWEEP_BY + threadIdx.y, z = blockIdx.z;
-  if (y >= ny) return;
-  const int w0 = 2 * blockIdx.x;
-  const long long trow = ((long long)z * ny + y) * a.nxw;
-  const bool act0 = !a.tile_slow[trow + w0];
-  const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
-  if (!act0 && !act1) return;  // whole warp
-  const int x0 = 32 * w0 + lane, x1 = x0 + 32;
+  const int x1 = x0 + 32;
   const bool st0 = act0 && x0 < nx, st1 = act1 && x1 < nx;
   const long long S = a.L.S;
   const long long c = a.L.idx(x0, y, z);
@@ -426,6 +420,20 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
     if (st0) SF::template store<float, L>(q + i * S, f[i].x, i);
     if (st1) SF::template store<float, L>(q + i * S + 32, f[i].y, i);
   }
+}
+
+template <int Q, class ST, int MINB>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
+    sweep_channel2_kernel(const SweepArgs a) {
+  const int ny = a.L.ny;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y, z = blockIdx.z;
+  if (y >= ny) return;
+  const int w0 = 2 * blockIdx.x;
+  const long long trow = ((long long)z * ny + y) * a.nxw;
+  const bool act0 = !a.tile_slow[trow + w0];
+  const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
+  if (!act0 && !act1) return;  // whole warp
+  channel2_cells<Q, ST>(a, 32 * w0 + threadIdx.x, y, z, act0, act1);
 }
 
 // Channel sweep.  BOUNDARY = false: every warp tile that is not listed (rows
