@@ -48,7 +48,7 @@ class Info(ctypes.Structure):
         ("pop_stride", ctypes.c_int64), ("steps_done", ctypes.c_int64),
         ("n_links", ctypes.c_int64), ("n_solid", ctypes.c_int64), ("omega", ctypes.c_double),
         ("bytes_per_cell_step", ctypes.c_double), ("device_bytes", ctypes.c_size_t),
-        ("layout", ctypes.c_int), ("interior_kernel", ctypes.c_int),
+        ("layout", ctypes.c_int),
     ]
 
 

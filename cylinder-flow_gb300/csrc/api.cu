@@ -63,8 +63,7 @@ void free_handle(cflbm_handle *h) {
   void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
                   h->d_links_bits, h->d_tile_slow, h->d_slow_tiles,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
-                  h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums,
-                  h->d_tma_tiles, h->d_err};
+                  h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
@@ -77,15 +76,6 @@ void free_handle(cflbm_handle *h) {
   if (h->fork.side) cudaStreamDestroy(h->fork.side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
-}
-
-// The device error flag: set by a bounded pipeline wait that expired.
-int check_device_flag(cflbm_handle *h) {
-  if (!h->d_err) return CFLBM_OK;
-  int v = 0;
-  CK_CUDA(cudaMemcpy(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (v) return fail(CFLBM_E_CUDA, "a pipelined sweep wait timed out (device flag %d)", v);
-  return CFLBM_OK;
 }
 
 int store_size(int storage) {
@@ -339,8 +329,6 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   CK_CUDA(cudaEventCreateWithFlags(&h->ev_sync, cudaEventDisableTiming));
   CK_CUDA(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, cfg->device));
-  CK_CUDA(cudaMalloc(&h->d_err, sizeof(int)));
-  CK_CUDA(cudaMemset(h->d_err, 0, sizeof(int)));
   if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
     // Side stream of the channel sweep's listed-tile kernel, at the highest
     // priority so its blocks are scheduled ahead of the interior kernel's.
@@ -444,7 +432,6 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     const std::vector<unsigned char> flag =
         solid_tiles(solid, bits, nx, ny, nz, h->nxw, list, tile_bits);
     h->n_slow = (int)list.size();
-    if ((rc = tma_setup(h, flag))) return rc;
     if ((rc = dev_alloc_t(h, &h->d_tile_slow, flag.size()))) return rc;
     CK_CUDA(cudaMemcpyAsync(h->d_tile_slow, flag.data(), flag.size(), cudaMemcpyHostToDevice,
                             h->stream));
@@ -621,18 +608,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   if (!ref) {
     const SweepArgs sa = channel_args(h, h->fA, h->fB, write_macros);
     if (h->timing && (trc = record_event(h, &ts0))) return trc;
-    if (h->tma) {
-      // Listed tiles on the side stream, the interior through the TMA pipeline.
-      const int src = h->fA == h->buf[0] ? 0 : 1;
-      CK_CUDA(cudaEventRecord(h->fork.fork, h->stream));
-      CK_CUDA(cudaStreamWaitEvent(h->fork.side, h->fork.fork, 0));
-      CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->fork.side, nullptr, false));
-      CK_CUDA(cudaEventRecord(h->fork.join, h->fork.side));
-      CK_CUDA(launch_sweep_tma(h, sa, src, h->stream));
-      CK_CUDA(cudaStreamWaitEvent(h->stream, h->fork.join, 0));
-    } else {
-      CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream, &h->fork));
-    }
+    CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream, &h->fork));
     if (h->timing) {
       if ((trc = record_event(h, &ts1))) return trc;
       h->sweep_ev.push_back({ts0, ts1});
@@ -745,7 +721,7 @@ int cflbm_synchronize(cflbm_handle *h) {
   CK_CUDA(cudaSetDevice(h->cfg.device));
   CK_CUDA(cudaStreamSynchronize(h->stream));
   CK_CUDA(cudaGetLastError());
-  return check_device_flag(h);
+  return CFLBM_OK;
 }
 
 int cflbm_macros(cflbm_handle *h, double *u, double *v, double *w, double *p) {
@@ -889,7 +865,6 @@ int cflbm_get_info(cflbm_handle *h, cflbm_info *info) {
   info->pitch_x = h->L.px;
   info->pop_stride = h->L.S;
   info->layout = h->cfg.layout;
-  info->interior_kernel = h->tma ? 1 : 0;
   info->steps_done = h->steps_done;
   info->n_links = h->n_links;
   info->n_solid = h->n_solid;

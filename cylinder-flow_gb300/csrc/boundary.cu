@@ -459,14 +459,14 @@ cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cuda
 }
 
 cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a, cudaStream_t s,
-                                     const SweepFork *fk, bool interior);
+                                     const SweepFork *fk);
 cudaError_t launch_sweep_channel_q27(int store, int compute, const SweepArgs &a, cudaStream_t s,
-                                      const SweepFork *fk, bool interior);
+                                      const SweepFork *fk);
 
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
-                                 cudaStream_t s, const SweepFork *fk, bool interior) {
-  return Q == 9 ? launch_sweep_channel_q9(store, compute, a, s, fk, interior)
-                : launch_sweep_channel_q27(store, compute, a, s, fk, interior);
+                                 cudaStream_t s, const SweepFork *fk) {
+  return Q == 9 ? launch_sweep_channel_q9(store, compute, a, s, fk)
+                : launch_sweep_channel_q27(store, compute, a, s, fk);
 }
 
 // Dispatch helper: run F<Q, ST> for the runtime (Q, store).

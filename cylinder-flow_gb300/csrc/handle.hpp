@@ -3,7 +3,6 @@
 #include <cstdint>
 #include <string>
 #include <vector>
-#include <cuda.h>
 #include <cuda_runtime.h>
 #include "../../include/cflbm.h"
 #include "solver.cuh"
@@ -56,14 +55,6 @@ struct cflbm_handle {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<std::pair<size_t, size_t>> sweep_ev, bnd_ev;
-  // TMA-fed interior sweep for FP16 storage (sweep_tma.cu): tiles, tensor map
-  // of each population buffer.
-  bool tma = false;
-  int4 *d_tma_tiles = nullptr;
-  int tma_tiles_n = 0;
-  int tma_grid = 0;
-  CUtensorMap tma_map[2];
-  int *d_err = nullptr;  // set by a bounded pipeline wait that expired
 };
 
 namespace cflbm {
@@ -84,11 +75,6 @@ double channel_area(const cflbm_config &c);
 
 // Channel-sweep arguments of a handle (api.cu).
 SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool write_macros);
-
-// TMA-fed interior sweep (sweep_tma.cu).
-int tma_setup(cflbm_handle *h, const std::vector<unsigned char> &row_listed);
-cudaError_t launch_sweep_tma(const cflbm_handle *h, const SweepArgs &a, int src, cudaStream_t s);
-int record_error(int code, const char *msg);
 
 // Tecplot binary writer (tecplot.cpp).
 int write_tecplot(const char *path, int dim, int nx, int ny, int nz, const double *u,

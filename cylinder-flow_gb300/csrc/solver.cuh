@@ -126,8 +126,7 @@ struct SweepFork {
   cudaEvent_t fork, join;
 };
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
-                                 cudaStream_t s, const SweepFork *fk = nullptr,
-                                 bool interior = true);
+                                 cudaStream_t s, const SweepFork *fk = nullptr);
 // Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z
 // (the solid-tile launch runs 4 listed warp tiles per block).
 constexpr int SWEEP_BX = 32, SWEEP_BY = 4;

@@ -598,16 +598,10 @@ void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) 
 }
 
 template <int Q, class ST, class A, int MINB_FAST, int MINB_SLOW>
-cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const SweepFork *fk,
-                                   bool interior) {
+cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const SweepFork *fk) {
   dim3 block(SWEEP_BX, SWEEP_BY, 1);
   dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
   const int sb = a.bnd_blocks;
-  if (!interior) {  // the listed tiles only (the caller runs the interior itself)
-    sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
-    count_launch(1);
-    return cudaGetLastError();
-  }
   if (fk && fk->side) {
     // The listed tiles go first on the (higher-priority) side stream, so their
     // latency-bound blocks overlap the interior kernel's streaming.

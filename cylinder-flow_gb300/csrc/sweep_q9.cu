@@ -21,19 +21,18 @@ cudaError_t launch_sweep_q9(int store, int compute, const SweepArgs &a, cudaStre
 }
 
 cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a,
-                                     cudaStream_t s, const SweepFork *fk,
-                                     bool interior) {
+                                     cudaStream_t s, const SweepFork *fk) {
   if (compute == COMPUTE_F64) {
     switch (store) {
-      case STORE_F64: return launch_sweep_channel_t<9, double, double, 4, 2>(a, s, fk, interior);
-      case STORE_F32: return launch_sweep_channel_t<9, float, double, 4, 2>(a, s, fk, interior);
-      case STORE_F16: return launch_sweep_channel_t<9, F16Dev, double, 4, 2>(a, s, fk, interior);
+      case STORE_F64: return launch_sweep_channel_t<9, double, double, 4, 2>(a, s, fk);
+      case STORE_F32: return launch_sweep_channel_t<9, float, double, 4, 2>(a, s, fk);
+      case STORE_F16: return launch_sweep_channel_t<9, F16Dev, double, 4, 2>(a, s, fk);
     }
   } else {
     switch (store) {
-      case STORE_F64: return launch_sweep_channel_t<9, double, float, 8, 4>(a, s, fk, interior);
-      case STORE_F32: return launch_sweep_channel_t<9, float, float, 8, 4>(a, s, fk, interior);
-      case STORE_F16: return launch_sweep_channel_t<9, F16Dev, float, 8, 4>(a, s, fk, interior);
+      case STORE_F64: return launch_sweep_channel_t<9, double, float, 8, 4>(a, s, fk);
+      case STORE_F32: return launch_sweep_channel_t<9, float, float, 8, 4>(a, s, fk);
+      case STORE_F16: return launch_sweep_channel_t<9, F16Dev, float, 8, 4>(a, s, fk);
     }
   }
   return cudaErrorInvalidValue;

@@ -96,7 +96,6 @@ typedef struct cflbm_info {
   double bytes_per_cell_step; /* algorithmic HBM bytes per cell update of the sweep */
   size_t device_bytes;  /* device memory held by the handle */
   int layout;           /* enum cflbm_layout */
-  int interior_kernel;  /* channel interior sweep: 0 = direct loads, 1 = TMA pipeline */
 } cflbm_info;
 
 /* Defaults: D2Q9 64x32, FP64 storage and arithmetic, CHANNEL, free-slip y,
