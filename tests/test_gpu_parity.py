@@ -181,7 +181,7 @@ def test_steps_are_deterministic_and_resumable(cuda):
 
 
 @pytest.mark.parametrize("name", ["d2q9_cyl_freeslip", "d3q27_cyl", "d3q27_noslip"])
-@pytest.mark.parametrize("storage", ["fp64", "fp16dev"])
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16dev"])
 def test_layouts_give_identical_states(cuda, name, storage):
     case = CHANNEL_CASES[name]
     steps = 60 if case["lattice"] == 9 else 12
