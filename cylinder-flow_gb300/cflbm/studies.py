@@ -310,13 +310,15 @@ def main():
     ap.add_argument("--precisions", default="fp32,fp64")
     ap.add_argument("--no-fd", action="store_true")
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--no-sequential", action="store_true",
+                    help="batch: skip the one-at-a-time FP64 comparison")
     args = ap.parse_args()
     if args.peak is None:
         args.peak = measured_peak_gbs()
     if args.study == "batch":
         steps = args.steps
         batch_study(args.instances, steps, window=steps // 2, peak_gbs=args.peak,
-                    out_path=args.out)
+                    out_path=args.out, sequential=not args.no_sequential)
         return
     if args.study == "adjoint":
         steps = args.steps if args.steps != 20000 else 7000
