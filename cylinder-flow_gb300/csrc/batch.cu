@@ -115,12 +115,7 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
         const long long trow = ((long long)z * ny + y) * a.nxw;
         const bool act0 = !a.tile_slow[trow + w0];
         const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
-        if (act0 || act1) {
-          if constexpr (std::is_same<ST, F16Dev>::value)
-            channel2h_cells<Q>(a, 32 * w0, y, z, act0, act1);
-          else
-            channel2_cells<Q, ST>(a, 32 * w0 + lane, y, z, act0, act1);
-        }
+        if (act0 || act1) channel2_cells<Q, ST>(a, 32 * w0 + lane, y, z, act0, act1);
       }
       continue;
     }

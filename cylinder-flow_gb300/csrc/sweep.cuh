@@ -87,20 +87,14 @@ __device__ __forceinline__ V acc_(V acc, V v) {
 //   c0 = rho3 - 1.5 |u|^2
 //   feq_{i,j} = ws_i (c0 + 4.5 (e.u)^2) +- 3 ws_i (e.u),  ws_i = w_i scale_i
 //   f <- f + omega (feq - f)
-// The populations are reached through an accessor: get(i) -> V, put(i, V).  An
-// array accessor keeps them in registers; the FP16 kernel's accessor keeps the
-// loaded halves packed and stores each result as soon as it is relaxed.
-template <class L, class V, class SF, class ACC>
-__device__ __forceinline__ void bgk_relax_acc(ACC &acc, V rho3, V ux, V uy, V uz, V om) {
+template <class L, class V, class SF>
+__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, V om) {
   using O = VA<V>;
   using S = typename O::S;
   const V usq = O::fma(ux, ux, O::fma(uy, uy, O::mul(uz, uz)));
   const V c0 = O::fma(O::splat(S(-1.5)), usq, rho3);
-  {
-    const V f0 = acc.get(0);
-    acc.put(0, O::fma(om, O::sub(O::mul(O::splat(S(L::w(0) * SF::template scale<L>(0))), c0), f0),
-                      f0));
-  }
+  f[0] = O::fma(om, O::sub(O::mul(O::splat(S(L::w(0) * SF::template scale<L>(0))), c0), f[0]),
+                f[0]);
   static_for(
       [&](auto kc) {
         constexpr int k = decltype(kc)::value;
@@ -121,24 +115,10 @@ __device__ __forceinline__ void bgk_relax_acc(ACC &acc, V rho3, V ux, V uy, V uz
         }
         const V sym = O::mul(O::splat(S(ws)), O::fma(O::splat(S(4.5)), O::mul(eu, eu), c0));
         const V asym = O::mul(O::splat(S(3.0 * ws)), eu);
-        const V fi = acc.get(i), fj = acc.get(j);
-        acc.put(i, O::fma(om, O::sub(O::add(sym, asym), fi), fi));
-        acc.put(j, O::fma(om, O::sub(O::sub(sym, asym), fj), fj));
+        f[i] = O::fma(om, O::sub(O::add(sym, asym), f[i]), f[i]);
+        f[j] = O::fma(om, O::sub(O::sub(sym, asym), f[j]), f[j]);
       },
       std::make_integer_sequence<int, L::NPAIR>{});
-}
-
-template <class V>
-struct ArrayAcc {
-  V *f;
-  __device__ V get(int i) const { return f[i]; }
-  __device__ void put(int i, V v) { f[i] = v; }
-};
-
-template <class L, class V, class SF>
-__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, V om) {
-  ArrayAcc<V> acc{f};
-  bgk_relax_acc<L, V, SF>(acc, rho3, ux, uy, uz, om);
 }
 
 template <class L, class A, class SF>
@@ -150,34 +130,27 @@ __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const 
 
 // Moments in deviation form: rho3 = 3p = sum f, u = sum f e, from populations
 // in storage units (the 1/scale factors are exact powers of two, 1 for FP32/64).
-template <class L, class V, class SF, class ACC>
-__device__ __forceinline__ void moments_acc(const ACC &acc, V &rho3, V &ux, V &uy, V &uz) {
+template <class L, class V, class SF>
+__device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
   using O = VA<V>;
   using S = typename O::S;
   constexpr int S0 = (int)SF::template scale<L>(0);
-  if constexpr (S0 == 1) rho3 = acc.get(0);
-  else rho3 = O::mul(acc.get(0), O::splat(S(1.0 / S0)));
+  if constexpr (S0 == 1) rho3 = f[0];
+  else rho3 = O::mul(f[0], O::splat(S(1.0 / S0)));
   ux = uy = uz = O::splat(S(0));
   static_for(
       [&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int i = L::pair(k), j = L::opp(L::pair(k));
         constexpr int SC = (int)SF::template scale<L>(i);
-        const V fi = acc.get(i), fj = acc.get(j);
-        const V sm = O::add(fi, fj);
-        const V d = O::sub(fi, fj);
+        const V sm = O::add(f[i], f[j]);
+        const V d = O::sub(f[i], f[j]);
         rho3 = acc_<V, 1, SC>(rho3, sm);
         if constexpr (L::ex(i) != 0) ux = acc_<V, L::ex(i), SC>(ux, d);
         if constexpr (L::ey(i) != 0) uy = acc_<V, L::ey(i), SC>(uy, d);
         if constexpr (L::ez(i) != 0) uz = acc_<V, L::ez(i), SC>(uz, d);
       },
       std::make_integer_sequence<int, L::NPAIR>{});
-}
-
-template <class L, class V, class SF>
-__device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
-  const ArrayAcc<V> acc{const_cast<V *>(f)};
-  moments_acc<L, V, SF>(acc, rho3, ux, uy, uz);
 }
 
 // Macros out (when requested), Brinkman damping of the equilibrium velocity,
@@ -390,104 +363,6 @@ __device__ __forceinline__ float2 pull_pair(const typename Store<ST>::elem *__re
   return make_float2(v0, v1);
 }
 
-// FP16 storage, adjacent cells: a warp owns the 64 cells of two warp tiles and
-// a thread the adjacent pair (x, x + 1), x = x0 + 2 lane, so every population
-// moves as one aligned 4-byte half2 per thread -- 128-byte warp requests, half
-// the load and store instructions of one cell per thread.  A direction with
-// e_x = +1 needs (src[x-1], src[x]): the left neighbour's word's high half
-// comes by warp shuffle (lane 0 loads it); e_x = -1 likewise from the right.
-// The populations stay packed as loaded (one register per direction); get()
-// widens them (the inlet column takes its FP32 equilibrium value), put() rounds
-// both cells with one conversion and stores them together.  The per-cell
-// operations and their order are those of every other kernel.
-template <int Q>
-struct PairAcc {
-  __half2 h[Q];
-  const SweepArgs &a;
-  bool inlet0, st0, st1;
-  __half *q;
-  long long S;
-  __device__ float2 get(int i) const {
-    float2 v = __half22float2(h[i]);
-    if (Lat<Q>::ex(i) > 0) v.x = inlet0 ? a.f_in_f[i] : v.x;
-    return v;
-  }
-  __device__ void put(int i, float2 v) {
-    const __half2 w = __floats2half2_rn(v.x, v.y);
-    __half *d = q + i * S;
-    if (st0 && st1) *reinterpret_cast<__half2 *>(d) = w;
-    else if (st0) d[0] = __low2half(w);
-    else if (st1) d[1] = __high2half(w);
-  }
-};
-
-// Cells x and x + 1 of row (y, z), x = x0 + 2 lane, x0 = 32 * even warp tile;
-// act0 / act1: the two warp tiles are unlisted (warp-uniform, one true).
-template <int Q>
-__device__ __forceinline__ void channel2h_cells(const SweepArgs &a, int x0, int y, int z,
-                                                bool act0, bool act1) {
-  using L = Lat<Q>;
-  using SF = Store<F16Dev>;
-  using O = VA<float2>;
-  const int nx = a.L.nx, ny = a.L.ny;
-  const int lane = threadIdx.x;
-  const int x = x0 + 2 * lane;
-  const bool act = lane < 16 ? act0 : act1;
-  const bool st0 = act && x < nx, st1 = act && x + 1 < nx;
-  const bool inlet0 = x == 0, out0 = x == nx - 1, out1 = x + 1 == nx - 1;
-  const long long S = a.L.S;
-  const long long c = a.L.idx(x, y, z);
-  const long long c0 = a.L.idx(x0, y, z);
-  const __half *__restrict__ fa = static_cast<const __half *>(a.fa);
-  PairAcc<Q> acc{{}, a, inlet0, st0, st1, static_cast<__half *>(a.fb) + c, S};
-  static_for(
-      [&](auto ic) {
-        constexpr int I = decltype(ic)::value;
-        constexpr int ex = L::ex(I);
-        // source row of direction I (shifted in y and z only), at this pair
-        const long long rowoff = I * S - (L::ey(I) * a.L.rs + L::ez(I) * a.L.zs);
-        const __half2 w = __ldg(reinterpret_cast<const __half2 *>(fa + c + rowoff));
-        if constexpr (ex == 0) {
-          acc.h[I] = w;
-        } else if constexpr (ex > 0) {  // (src[x-1], src[x])
-          __half left = __high2half(__shfl_up_sync(0xffffffffu, w, 1));
-          if (lane == 0) left = __ldg(fa + c0 + rowoff - 1);
-          acc.h[I] = __halves2half2(left, __low2half(w));
-        } else {  // (src[x+1], src[x+2]); the outlet column repeats itself
-          __half right = __low2half(__shfl_down_sync(0xffffffffu, w, 1));
-          if (lane == 31) right = __ldg(fa + c0 + rowoff + 64);
-          acc.h[I] = __halves2half2(out0 ? __low2half(w) : __high2half(w),
-                                    out1 ? __high2half(w) : right);
-        }
-      },
-      std::make_integer_sequence<int, Q>{});
-  float2 rho3, ux, uy, uz;
-  moments_acc<L, float2, SF>(acc, rho3, ux, uy, uz);
-  const long long cell0 = ((long long)z * ny + y) * nx + x;
-  if (a.mu) {
-    if (st0) {
-      a.mu[cell0] = f2d_bits(ux.x);
-      a.mv[cell0] = f2d_bits(uy.x);
-      a.mw[cell0] = f2d_bits(uz.x);
-      a.mp[cell0] = f2d_bits(__fmul_rn(rho3.x, 1.0f / 3.0f));
-    }
-    if (st1) {
-      a.mu[cell0 + 1] = f2d_bits(ux.y);
-      a.mv[cell0 + 1] = f2d_bits(uy.y);
-      a.mw[cell0 + 1] = f2d_bits(uz.y);
-      a.mp[cell0 + 1] = f2d_bits(__fmul_rn(rho3.y, 1.0f / 3.0f));
-    }
-  }
-  if (a.alpha) {
-    const float2 sb = make_float2(__fsub_rn(1.0f, st0 ? a.alpha[cell0] : 0.0f),
-                                  __fsub_rn(1.0f, st1 ? a.alpha[cell0 + 1] : 0.0f));
-    ux = O::mul(ux, sb);
-    uy = O::mul(uy, sb);
-    uz = O::mul(uz, sb);
-  }
-  bgk_relax_acc<L, float2, SF>(acc, rho3, ux, uy, uz, O::splat(a.omega_f));
-}
-
 // Cells x0 and x0 + 32 of row (y, z) (x0 = 32 * even warp tile + lane); act0 /
 // act1: the two warp tiles are unlisted (warp-uniform).
 template <int Q, class ST>
@@ -507,7 +382,6 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
   const E *__restrict__ pm0 = p - (x0 == nx - 1 ? 1 : 0);
   const E *__restrict__ pm1 = p + 32 - (x1 == nx - 1 ? 1 : 0);
   const bool inlet0 = x0 == 0;
-
   float2 f[Q];
   static_for(
       [&](auto ic) {
@@ -559,10 +433,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
   const bool act0 = !a.tile_slow[trow + w0];
   const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
   if (!act0 && !act1) return;  // whole warp
-  if constexpr (std::is_same<ST, F16Dev>::value)
-    channel2h_cells<Q>(a, 32 * w0, y, z, act0, act1);
-  else
-    channel2_cells<Q, ST>(a, 32 * w0 + threadIdx.x, y, z, act0, act1);
+  channel2_cells<Q, ST>(a, 32 * w0 + threadIdx.x, y, z, act0, act1);
 }
 
 // Channel sweep.  BOUNDARY = false: every warp tile that is not listed (rows
