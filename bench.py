@@ -233,7 +233,7 @@ def run_gb300(args):
             extra[name] = {k: round(x, 4) if isinstance(x, float) else x for k, x in v.items()}
 
     # ---- end to end through the C ABI with host buffers --------------------------
-    e2e_steps = max(steps // 2, 10)
+    e2e_steps = max(steps, 10)  # as many steps as the device-timed leg
     solid = np.zeros((NZ, NY, NX), np.uint8)
     yy, xx = np.mgrid[0:NY, 0:NX]
     solid[:, ((xx - 128.0) ** 2 + (yy - 64.0) ** 2) <= (D / 2) ** 2] = 1

@@ -86,13 +86,24 @@ void LBM::Initialize() {
   fetched_step_ = -1;
 }
 
-void LBM::Collision() { check(cflbm_step(h_, 1), "cflbm_step"); }
+void LBM::Collision() {
+  if (++pending_ >= 1024) flush_forces();  // runs the queued steps first
+}
+
+void LBM::flush_steps() {
+  if (pending_ > 0 && h_) {
+    const int n = pending_;
+    pending_ = 0;
+    check(cflbm_step(h_, n), "cflbm_step");
+  }
+}
 
 void LBM::Streaming() {}
 
 void LBM::Update() {}
 
 const std::vector<double> &LBM::field(int which) {
+  flush_steps();
   cflbm_info info;
   check(cflbm_get_info(h_, &info), "cflbm_get_info");
   if (fetched_step_ != info.steps_done) {
@@ -108,6 +119,7 @@ const std::vector<double> &LBM::field(int which) {
 // "MPI Kokkos/lbm.cpp:398-407": every step appends "Cd Cl" (fixed, 17 digits)
 // to test.dat.  Kept on the GPU and appended in bulk here.
 void LBM::flush_forces() {
+  flush_steps();
   if (dim != 2 || !h_) return;
   cflbm_info info;
   check(cflbm_get_info(h_, &info), "cflbm_get_info");

@@ -7,10 +7,14 @@
 //        LBM(MPI_Comm, int sx, int sy, double &tau, double &rho0, double &u0)
 // so the reference's main() drives it unchanged.  All state lives on the GPU
 // behind the C ABI (include/cflbm.h); the rank count is one, so
-// setup_subdomain/pack/exchange/unpack do nothing.  Collision() advances one
-// fused time step (collide + stream + boundaries + macroscopic update);
-// Streaming() and Update() then only do the host-side bookkeeping the reference
-// does at those points (the 2-D per-step "Cd Cl" record of test.dat).
+// setup_subdomain/pack/exchange/unpack do nothing.  Collision() accounts for one
+// fused time step (collide + stream + boundaries + macroscopic update); the steps
+// are queued and run together -- one cflbm_step call, replayed from CUDA graphs
+// -- when a result is needed (MPIoutput, Output, the fields, test.dat, the
+// handle) or every 1024 steps, so a main loop that steps one at a time runs as
+// fast as one that asks for many steps.  Streaming() and Update() do nothing
+// more; the 2-D per-step "Cd Cl" record of test.dat is kept on the GPU and
+// appended in bulk.
 //
 // ua/va/wa/p are host views of the macroscopic fields with the reference's
 // ghost-inclusive indexing (ua(i,j,k) with i in [ghost, lx-ghost)); they are
@@ -84,13 +88,19 @@ struct LBM {
   void MPIoutput(int n);
   void Output(int n);
 
-  cflbm_handle *handle() const { return h_; }
+  // The handle, with every queued step run.
+  cflbm_handle *handle() {
+    flush_steps();
+    return h_;
+  }
   const std::vector<double> &field(int which);
 
  private:
   void check(int rc, const char *what);
   void flush_forces();
+  void flush_steps();
   cflbm_handle *h_ = nullptr;
+  int pending_ = 0;  // steps accounted for by Collision() and not yet run
   std::vector<double> f_[4];
   int64_t fetched_step_ = -1;
   int64_t forces_flushed_ = 0;
