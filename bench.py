@@ -16,6 +16,9 @@ host buffers, step, read every step's force (Cd, Cl) back to the host as the
 reference's test.dat loop does, and read the final u, v, w, p fields back.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--workload channel2d` measures the small D2Q9 400x100 channel instead, over its
+whole 20,000-step run, in every storage form, with the run's Cd, Cl and St.
 """
 from __future__ import annotations
 
@@ -295,6 +298,143 @@ def run_gb300(args):
     return 0
 
 
+# ---- the small channel problem: D2Q9 400x100 cylinder, 20,000 steps ---------------
+# Cylinder D = 20 at (80, 50), equilibrium inlet u = (0.05, 0), zero-gradient
+# outlet, free-slip walls, Re = 100 (tau = 0.5 + 3 u D / Re), seeded +-1e-3 u_y
+# perturbation; Cd, Cl and St over the last 10,000 steps.  40,000 cells: the
+# whole state (2 x 2.9 MB in FP64) stays in L2, so a step is bound by launch and
+# latency, not by HBM.
+CH2D = dict(lattice=9, nx=400, ny=100, tau0=3 * 0.05 * 20 / 100, u0=0.05, wall_y="freeslip",
+            geom="cylinder", cx=80.0, cy=50.0, diam=20.0, perturb_amp=1e-3, seed=1234)
+CH2D_CELLS = 400 * 100
+CH2D_WINDOW = 10000
+METRIC_2D = "MLUPS (D2Q9 BGK sweep, 400x100 cylinder channel, 20,000-step run)"
+
+
+def run_channel2d(args):
+    """Every storage/arithmetic form over the full 20,000-step run, device time
+    from t = 0 (the warm-up steps run first and the state is then reset to the
+    initial one), the run's Cd mean, Cl rms and St, and the plain FP64 form end
+    to end from host buffers."""
+    world, rank, local = dist_setup(args)
+    import torch
+    import cflbm
+    from cflbm import analysis
+
+    peak, peak_kind = peaks()
+    steps, warmup = args.steps, args.warmup
+    forms = {}
+    n_launch = 0
+    with ClockSampler(local) as clk:
+        for name, st, cp in (("fp64", "fp64", "fp64"), ("fp64_store", "fp64", "fp32"),
+                             ("fp32_store", "fp32", "fp32"), ("fp16dev_store", "fp16dev", "fp32")):
+            with cflbm.Solver(device=local, storage=st, compute=cp, force_history=steps + 8,
+                              **CH2D) as s:
+                stream = torch.cuda.ExternalStream(s.stream_ptr())
+                f0 = s.get_f()
+                s.step(warmup)
+                s.set_f(f0, 0)
+                s.synchronize()
+                barrier(world)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                l0 = cflbm.launch_count()
+                e0.record(stream)
+                s.step(steps)
+                e1.record(stream)
+                e1.synchronize()
+                launches = cflbm.launch_count() - l0
+                ms = max_over_ranks(e0.elapsed_time(e1), world)
+                hist = s.force_history(steps)
+                stats = analysis.summary(hist, CH2D["u0"], CH2D["diam"], CH2D["diam"],
+                                         min(CH2D_WINDOW, steps))
+                info = s.info()
+            if name == "fp64":
+                n_launch = launches
+            forms[name] = {"mlups": round(world * CH2D_CELLS * steps / (ms * 1e-3) / 1e6, 2),
+                           "us_per_step": round(1e3 * ms / steps, 3),
+                           "bytes_per_cell": info.bytes_per_cell_step,
+                           "cd_mean": stats["cd_mean"], "cl_rms": stats["cl_rms"],
+                           "st": stats["st"]}
+    ref = forms["fp64"]
+    for v in forms.values():
+        v["cd_rel_err"] = abs(v["cd_mean"] - ref["cd_mean"]) / abs(ref["cd_mean"])
+        v["st_rel_err"] = abs(v["st"] - ref["st"]) / abs(ref["st"]) if ref["st"] else None
+
+    # ---- end to end, plain FP64 form: solid mask from the host, the run, the
+    # force history and the final u, v, w, p fields back to the host --------------
+    solid = np.zeros((1, CH2D["ny"], CH2D["nx"]), np.uint8)
+    yy, xx = np.mgrid[0:CH2D["ny"], 0:CH2D["nx"]]
+    solid[0, ((xx - CH2D["cx"]) ** 2 + (yy - CH2D["cy"]) ** 2) <= (CH2D["diam"] / 2) ** 2] = 1
+    wl = dict(CH2D)
+    wl["geom"] = "none"
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with cflbm.Solver(device=local, storage="fp64", compute="fp64", solid=solid,
+                      force_history=steps + 8, **wl) as s:
+        s.step(steps)
+        hist = s.force_history(steps)
+        u, v, w, p = s.macros()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": round(world * CH2D_CELLS * steps / e2e_s / 1e6, 2), "unit": "MLUPS",
+           "h2d_bytes_per_step": solid.nbytes / steps,
+           "d2h_bytes_per_step": (hist.nbytes + u.nbytes + v.nbytes + w.nbytes + p.nbytes) / steps,
+           "steps": steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_2d(args.cpu_steps_2d)
+    bpc = ref["bytes_per_cell"]
+    achieved = bpc * CH2D_CELLS / (ref["us_per_step"] * 1e-6) / 1e9
+    line = {
+        "metric": METRIC_2D, "value": ref["mlups"], "unit": "MLUPS", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": round(ref["us_per_step"] / 1e3, 6),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded perturbation; no dataset)",
+        "config": {"workload": "D2Q9 400x100 cylinder channel D=20, Re=100, free-slip walls, "
+                               "20,000 steps (BASELINE configs[0])",
+                   "storage": "f64", "collision": "f64", "global_cells": CH2D_CELLS * world,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "working set 2 x 2.9 MB, L2-resident (the problem's own size)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": peak_kind, "bytes_per_cell": bpc,
+                     "note": "L2-resident and launch-bound: two launches per step"},
+        "e2e": e2e, "gpu_launches": n_launch, "clocks": clk.summary(), "forms": forms,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def cpu_baseline_2d(steps: int):
+    """The reference's 2-D solver on the host cores: the oracle port of its D2Q9
+    passes (serial Update loop and force sum included) at 400x100, OpenMP over
+    all cores, over a bounded number of steps."""
+    from oracle import oracle as O
+    import ctypes
+    cores = os.cpu_count() or 1
+    L = O.lib()
+    nx, ny = CH2D["nx"], CH2D["ny"]
+    ran = np.zeros((nx + 4) * (ny + 4), np.int32)
+    t0 = time.perf_counter()
+    rc = L.oracle_ref2d_run(nx, ny, CH2D["tau0"], CH2D["u0"],
+                            ran.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), steps,
+                            None, None, None, None, None, None, cores)
+    dt = time.perf_counter() - t0
+    assert rc == 0
+    return {"value": round(CH2D_CELLS * steps / max(dt, 1e-9) / 1e6, 3), "unit": "MLUPS",
+            "cores": cores, "kind": "port",
+            "sample": f"{steps} of the 20,000 steps of the 400x100 D2Q9 grid (reference "
+                      f"solver structure incl. its serial Update loop and force sum)"}
+
+
 def cpu_baseline(steps: int):
     """The reference's algorithm on the host cores: the oracle port of the 3-D
     reference solver (same passes, same serial Update loop) at 512x128x128,
@@ -325,17 +465,20 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    two_d = args.workload == "channel2d"
     runs = []
     for _ in range(max(args.steps_ref, 1)):
-        runs.append(cpu_baseline(args.cpu_steps))
+        runs.append(cpu_baseline_2d(args.cpu_steps_2d) if two_d else cpu_baseline(args.cpu_steps))
     v = statistics.median(r["value"] for r in runs)
     cb = dict(runs[0])
     cb["value"] = v
     line = {
-        "metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": world, "steps": args.steps_ref,
+        "metric": METRIC_2D if two_d else METRIC, "value": v, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps_ref,
         "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": "D3Q27 512x128x128 (reference solver on the host cores)"},
+        "config": {"workload": ("D2Q9 400x100" if two_d else "D3Q27 512x128x128")
+                               + " (reference solver on the host cores)"},
         "cpu_baseline": cb,
         "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -368,12 +511,17 @@ def run_profile(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--workload", default="cylinder3d", choices=["cylinder3d", "channel2d"],
+                    help="cylinder3d: D3Q27 512x128x128 (the benchmark line); channel2d: "
+                         "D2Q9 400x100 over its 20,000-step run")
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 1000; 20000 for channel2d)")
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline variant only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps-2d", type=int, default=4000)
     ap.add_argument("--profile", action="store_true",
                     help="bare stepping loop on an --nx/--ny/--nz grid for profiler captures")
     ap.add_argument("--nx", type=int, default=NX)
@@ -384,12 +532,16 @@ def main():
     ap.add_argument("--layout", default="rows", choices=["soa", "rows"])
     args = ap.parse_args()
     args.steps_ref = 1
+    if args.steps is None:
+        args.steps = 20000 if args.workload == "channel2d" else 1000
     if args.warmup < 3:
         args.warmup = 3
     if args.profile:
         return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "channel2d":
+        return run_channel2d(args)
     return run_gb300(args)
 
 
