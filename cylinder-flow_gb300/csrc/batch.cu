@@ -82,11 +82,17 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
   // Each block takes a contiguous range of work items (items are ordered by
   // instance, then z, y, x), so the instance's arguments are staged in shared
   // memory only when the range crosses into the next instance.
+  // The next item is loaded one iteration ahead, so an item's population loads
+  // wait for nothing else.
   const int w0 = (int)((long long)blockIdx.x * n_work / gridDim.x);
   const int w1 = (int)((long long)(blockIdx.x + 1) * n_work / gridDim.x);
   int staged = -1;
+  int4 wn = w0 < w1 ? work[w0] : make_int4(0, 0, 0, 0);
   for (int w = w0; w < w1; ++w) {
-    const int4 wk = work[w];  // (instance, x tile, y tile | listed block, z)
+    // (instance, x pair | row flags << 16, y tile, z) for fast items,
+    // (instance, 0, listed block, 0) for solid items
+    const int4 wk = wn;
+    if (w + 1 < w1) wn = work[w + 1];
     if (wk.x != staged) {     // block-uniform
       __syncthreads();
       const int *src = reinterpret_cast<const int *>(args + 4 * (long long)wk.x + sel);
@@ -108,15 +114,15 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
       z = row / ny;
       x = (tile % a.nxw) * 32 + lane;
     } else {
+      // Bits 2r and 2r + 1 of the row flags: warp tiles 2 * pair and 2 * pair + 1
+      // of row r of the item are unlisted (and inside the box).
       y = wk.z * BY + wid;
       z = wk.w;
-      const int w0 = 2 * wk.y;
-      if (y < ny) {  // warp-uniform
-        const long long trow = ((long long)z * ny + y) * a.nxw;
-        const bool act0 = !a.tile_slow[trow + w0];
-        const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
-        if (act0 || act1) channel2_cells<Q, ST>(a, 32 * w0 + lane, y, z, act0, act1);
-      }
+      const int pair = wk.y & 0xffff;
+      const unsigned rf = ((unsigned)wk.y >> 16) >> (2 * wid);
+      const bool act0 = rf & 1u, act1 = (rf >> 1) & 1u;
+      if (act0 || act1)  // warp-uniform
+        channel2_cells<Q, ST>(a, 64 * pair + lane, y, z, act0, act1);
       continue;
     }
     double Fx = 0.0, Fy = 0.0, Fz = 0.0;
@@ -359,6 +365,13 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
   }
   BCK(cudaMalloc(&b->d_args, args.size() * sizeof(SweepArgs)));
   BCK(cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice));
+  // Per-tile listed flags of every instance, read back once.
+  std::vector<std::vector<unsigned char>> slow(n);
+  for (int k = 0; k < n; ++k) {
+    const cflbm_handle *h = b->inst[k];
+    slow[k].resize((size_t)h->nxw * h->L.ny * h->L.nz);
+    BCK(cudaMemcpy(slow[k].data(), h->d_tile_slow, slow[k].size(), cudaMemcpyDeviceToHost));
+  }
   // Work lists per tile-height candidate.
   for (int ci = 0; ci < 4; ++ci) {
     const int by = BY_CANDIDATES[ci];
@@ -366,9 +379,22 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
     for (int k = 0; k < n; ++k) {
       const cflbm_handle *h = b->inst[k];
       const int gx = (h->nxw + 1) / 2, gy = (h->L.ny + by - 1) / by;  // 64-cell items
+      const int nxw = h->nxw, ny = h->L.ny;
+      // Items carry the unlisted flags of their warp tiles (two per row), so
+      // the kernel reads no per-tile flag; items with no unlisted tile are left out.
       for (int z = 0; z < h->L.nz; ++z)
         for (int yb = 0; yb < gy; ++yb)
-          for (int xb = 0; xb < gx; ++xb) wf.push_back(make_int4(k, xb, yb, z));
+          for (int xb = 0; xb < gx; ++xb) {
+            unsigned rf = 0;
+            for (int r = 0; r < by; ++r) {
+              const int y = yb * by + r;
+              if (y >= ny) break;
+              const size_t row = ((size_t)z * ny + y) * nxw;
+              if (!slow[k][row + 2 * xb]) rf |= 1u << (2 * r);
+              if (2 * xb + 1 < nxw && !slow[k][row + 2 * xb + 1]) rf |= 2u << (2 * r);
+            }
+            if (rf) wf.push_back(make_int4(k, xb | (int)(rf << 16), yb, z));
+          }
       const int nb = (h->n_slow + by - 1) / by;
       for (int q = 0; q < std::max(nb, 1); ++q) ws.push_back(make_int4(k, 0, q, 0));  // .z = listed block
     }
