@@ -207,18 +207,42 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
   }
 }
 
+// Fast items, one per block: the block reads its item and its instance's
+// arguments straight from global memory (cached in L1; no shared-memory staging
+// and no barrier), and the hardware scheduler keeps the SMs full.
+template <int Q, class ST, int BY>
+__global__ void __launch_bounds__(32 * BY, 24 / BY)
+    batch_fast_kernel(const SweepArgs *__restrict__ args, const int4 *__restrict__ work, int sel) {
+  const int4 wk = work[blockIdx.x];  // (instance, x pair | row flags << 16, y tile, z)
+  const SweepArgs &a = args[4 * (long long)wk.x + sel];
+  const int wid = threadIdx.y;
+  const unsigned rf = ((unsigned)wk.y >> 16) >> (2 * wid);
+  const bool act0 = rf & 1u, act1 = (rf >> 1) & 1u;
+  if (act0 || act1)  // warp-uniform
+    channel2_cells<Q, ST>(a, 64 * (wk.y & 0xffff) + threadIdx.x, wk.z * BY + wid, wk.w, act0,
+                          act1);
+}
+
+// grid > 0: persistent grids of `grid` blocks for both kinds of work; grid = 0:
+// one fast item per block, and the solid work on two blocks per SM.
 template <int Q, class ST, int BY>
 cudaError_t launch_batch_t(const cflbm_batch *b, int kind, int sel, int grid, cudaStream_t s) {
   const int ci = BY == 1 ? 0 : BY == 2 ? 1 : BY == 4 ? 2 : 3;
   dim3 block(32, BY, 1);
   if (kind == 0) {
-    if (b->n_work_fast[ci] > 0)
-      batch_sweep_kernel<Q, ST, float, BY, false>
-          <<<std::min(grid, b->n_work_fast[ci]), block, 0, s>>>(b->d_args, b->d_work_fast[ci],
-                                                                b->n_work_fast[ci], sel);
+    if (b->n_work_fast[ci] > 0) {
+      if (grid > 0)
+        batch_sweep_kernel<Q, ST, float, BY, false>
+            <<<std::min(grid, b->n_work_fast[ci]), block, 0, s>>>(b->d_args, b->d_work_fast[ci],
+                                                                  b->n_work_fast[ci], sel);
+      else
+        batch_fast_kernel<Q, ST, BY><<<b->n_work_fast[ci], block, 0, s>>>(
+            b->d_args, b->d_work_fast[ci], sel);
+    }
   } else {
+    const int g = grid > 0 ? grid : 2 * b->sms;
     batch_sweep_kernel<Q, ST, float, BY, true>
-        <<<std::max(1, std::min(grid, b->n_work_solid[ci])), block, 0, s>>>(
+        <<<std::max(1, std::min(g, b->n_work_solid[ci])), block, 0, s>>>(
             b->d_args, b->d_work_solid[ci], b->n_work_solid[ci], sel);
   }
   count_launch();
@@ -409,14 +433,14 @@ int cflbm_batch_create(const cflbm_config *cfgs, int n, const cflbm_batch_option
   // the real state without advancing it (A -> B, no swap), then restores the
   // force-history counters.
   b->by = o.tile_height;
-  b->grid = std::max(1, o.blocks_per_sm) * sms;
+  b->grid = std::max(0, o.blocks_per_sm) * sms;
   if (o.autotune) {
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
     float best = 1e30f;
     for (int ci = 0; ci < 4; ++ci)
-      for (int bps : {2, 3, 4, 6, 8, 12, 16}) {
+      for (int bps : {0, 2, 3, 4, 6, 8, 12, 16}) {  // 0: one fast item per block
         const int by = BY_CANDIDATES[ci];
         if (32 * by * bps > 2048) continue;
         const int grid = bps * sms;

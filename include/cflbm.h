@@ -187,7 +187,8 @@ typedef struct cflbm_batch_options {
   int graph_steps;    /* steps per captured graph (even, default 100) */
   int autotune;       /* 1 (default): time candidates at creation */
   int tile_height;    /* rows per block when not autotuning: 1, 2, 4 or 8 */
-  int blocks_per_sm;  /* persistent grid = SMs * this when not autotuning */
+  int blocks_per_sm;  /* persistent grid = SMs * this when not autotuning; 0 = one
+                         interior work item per block */
 } cflbm_batch_options;
 
 typedef struct cflbm_batch_info {
@@ -195,7 +196,7 @@ typedef struct cflbm_batch_info {
   int64_t cells;               /* interior cells over all instances */
   int64_t steps_done;
   int tile_height;             /* chosen launch shape */
-  int grid_blocks;
+  int grid_blocks;             /* persistent grid, 0 = one interior item per block */
   int graph_steps;
   int tuned_candidates;        /* launch shapes timed by the autotuner */
   double tuned_step_ms;        /* best candidate's step time */

@@ -70,3 +70,30 @@ def test_batch_instance_cannot_be_stepped_alone(cuda):
             inst.step(1)
         with pytest.raises(IndexError):
             b.instance(5)
+
+
+def test_batch_launch_shapes_agree(cuda):
+    """One fast item per block (blocks_per_sm = 0) and persistent grids give the
+    same states for every tile height, and the same forces for one tile height
+    (force partials are per listed block, summed in block order)."""
+    cfgs = configs()
+    steps = 9
+    ref_f = None
+    for th in (1, 2, 4, 8):
+        out = []
+        for bps in (0, 3):
+            with Batch(cfgs, graph_steps=4, autotune=False, tile_height=th,
+                       blocks_per_sm=bps) as b:
+                assert (b.info().grid_blocks == 0) == (bps == 0)
+                b.step(steps)
+                b.synchronize()
+                out.append([(b.instance(k).get_f(), b.instance(k).force_history())
+                            for k in range(len(cfgs))])
+        for k in range(len(cfgs)):
+            assert np.array_equal(out[0][k][0], out[1][k][0]), (th, k)
+            assert np.array_equal(out[0][k][1], out[1][k][1]), (th, k)
+            if ref_f is None:
+                continue
+            assert np.array_equal(out[0][k][0], ref_f[k]), (th, k)
+        if ref_f is None:
+            ref_f = [out[0][k][0] for k in range(len(cfgs))]
