@@ -229,7 +229,9 @@ def batch_cases(n=64, seed=2025, u0=0.05):
 
 
 def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=None,
-                out_path=None, sequential=True):
+                out_path=None, sequential=True, shape=None):
+    """`shape` = (tile height, blocks per SM) fixes the launch shape instead of
+    autotuning it (blocks per SM 0: one interior work item per block)."""
     from .solver import Batch
     if peak_gbs is None:
         peak_gbs = measured_peak_gbs()
@@ -239,8 +241,10 @@ def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=None,
     res = {"instances": n, "steps": steps, "graph_steps": graph_steps, "cells": cells,
            "cases": cases}
     t0 = time.perf_counter()
+    kw = dict(autotune=True) if shape is None else dict(
+        autotune=False, tile_height=shape[0], blocks_per_sm=shape[1])
     with Batch([dict(c, storage="fp32", compute="fp32", force_history=steps + 8)
-                for c in cfgs], graph_steps=graph_steps, autotune=True) as b:
+                for c in cfgs], graph_steps=graph_steps, **kw) as b:
         t_create = time.perf_counter() - t0
         b.step(graph_steps)  # first replay captures the graph
         b.synchronize()
@@ -312,13 +316,17 @@ def main():
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-sequential", action="store_true",
                     help="batch: skip the one-at-a-time FP64 comparison")
+    ap.add_argument("--shape", default=None,
+                    help="batch: fixed launch shape 'tile_height,blocks_per_sm' instead of "
+                         "autotuning (blocks_per_sm 0: one interior item per block)")
     args = ap.parse_args()
     if args.peak is None:
         args.peak = measured_peak_gbs()
     if args.study == "batch":
         steps = args.steps
+        shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
         batch_study(args.instances, steps, window=steps // 2, peak_gbs=args.peak,
-                    out_path=args.out, sequential=not args.no_sequential)
+                    out_path=args.out, sequential=not args.no_sequential, shape=shape)
         return
     if args.study == "adjoint":
         steps = args.steps if args.steps != 20000 else 7000
