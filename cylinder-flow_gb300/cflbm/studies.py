@@ -19,8 +19,8 @@ the FP64 solver for u_in, tau and 16 seeded porosity directions.
 
 batch_study: the batched form (64 D2Q9 cylinder channels, widths 256-1024 and
 heights 64-256 in multiples of 32, D in [8, 32], Re in [40, 200], u_in = 0.05,
-FP32 storage, 20000 steps in one persistent launch per step replayed from a
-100-step CUDA graph, autotuned launch shape) against the same channels run one
+FP32 storage, 20000 steps in one launch per step over all channels, replayed
+from a 100-step CUDA graph, autotuned launch shape) against the same channels run one
 at a time with FP64 storage and arithmetic; per-instance Cd error against that
 FP64 run.
 

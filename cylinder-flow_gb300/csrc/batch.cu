@@ -1,21 +1,23 @@
 // Batched channels: many independent channel instances of uneven size and
-// Reynolds number advanced together, one persistent work-list launch per sweep
-// kind per step, replayed from a captured CUDA graph, with the launch shape
-// (tile height, persistent grid size) picked by a timing autotuner at creation.
+// Reynolds number advanced together, one work-list launch per sweep kind per
+// step over all instances, replayed from a captured CUDA graph, with the launch
+// shape (tile height; one interior item per block or a persistent grid size)
+// picked by a timing autotuner at creation.
 //
 // Each instance is an ordinary channel-profile handle (its own buffers, mask,
 // solid-tile list, force history), so every per-instance result call of the C ABI
 // works on cflbm_batch_handle(b, k).  The batch adds:
 //   * a device table of per-instance sweep arguments, one per A/B parity and
 //     macro flag;
-//   * a work list of (instance, tile block) items for the interior launch and
-//     one for the solid-tile launch (blocks of `by` listed tiles of one instance);
-//   * two persistent kernels that walk the lists with a grid-stride loop, copying
-//     the instance's arguments to shared memory per item and running the same
-//     per-cell code as the single-channel sweep (pull_plain/pull_resolved, moments,
-//     finish_cell); the solid kernel reduces each instance's body force into
-//     that instance's history, the last block of the instance summing its
-//     partials in block order.
+//   * a work list of (instance, tile block) items for the interior launch, each
+//     carrying its warp tiles' unlisted flags, and one for the solid-tile launch
+//     (blocks of `by` listed tiles of one instance);
+//   * the interior kernels (one item per block, or a persistent grid walking
+//     contiguous ranges of items) and the persistent solid kernel, running the
+//     same per-cell code as the single-channel sweep (channel2_cells,
+//     pull_resolved, moments, finish_cell); the solid kernel reduces each
+//     instance's body force into that instance's history, the last block of the
+//     instance summing its partials in block order.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -209,9 +211,12 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
 
 // Fast items, one per block: the block reads its item and its instance's
 // arguments straight from global memory (cached in L1; no shared-memory staging
-// and no barrier), and the hardware scheduler keeps the SMs full.
-template <int Q, class ST, int BY>
-__global__ void __launch_bounds__(32 * BY, 24 / BY)
+// and no barrier), and the hardware scheduler keeps the SMs full.  The launch
+// is latency-bound, so it is held to 48 registers (40 warps per SM, no spill);
+// measured on the 64-channel problem: 0.889 of the copy peak against 0.822 at
+// 59 registers and 0.881 at 40 registers (a 24-byte spill).
+template <int Q, class ST, int BY, int MINB = 40 / BY>
+__global__ void __launch_bounds__(32 * BY, MINB)
     batch_fast_kernel(const SweepArgs *__restrict__ args, const int4 *__restrict__ work, int sel) {
   const int4 wk = work[blockIdx.x];  // (instance, x pair | row flags << 16, y tile, z)
   const SweepArgs &a = args[4 * (long long)wk.x + sel];
