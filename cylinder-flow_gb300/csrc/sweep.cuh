@@ -588,10 +588,18 @@ void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) 
     // Blocks per SM, measured on the D3Q27 bench step: FP32 storage 0.850 /
     // 0.908 / 0.937 of the copy peak at 4 / 5 / 6 per SM (80 registers, no
     // spills at 6; 7 and 8 spill); FP16 0.613 / 0.636 / 0.632 (96 registers
-    // and a 44-byte spill at 5).
+    // and a 44-byte spill at 5).  D2Q9 on grids of 2^20 cells and more: 10 per
+    // SM (48 registers, no spill; 8192x1024: FP32 storage 0.982 against 0.946
+    // at 6, FP16 0.729 against 0.659); on smaller grids, which are bound by
+    // per-thread latency, 6 (640x160 FP32: 6.1 us per step against 6.6 at 10).
     constexpr int M2 = std::is_same<ST, float>::value ? 6 : 5;
     dim3 g2((a.nxw + 1) / 2, grid.y, grid.z);
-    sweep_channel2_kernel<Q, ST, M2><<<g2, block, 0, s>>>(a);
+    bool wide = false;
+    if constexpr (Q == 9) {
+      wide = (long long)a.L.nx * a.L.ny * a.L.nz >= (1LL << 20);
+      if (wide) sweep_channel2_kernel<Q, ST, 10><<<g2, block, 0, s>>>(a);
+    }
+    if (!wide) sweep_channel2_kernel<Q, ST, M2><<<g2, block, 0, s>>>(a);
   } else {
     sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
   }

@@ -17,7 +17,7 @@ from conftest import load_golden, rel_err
 from oracle import oracle as O
 
 import cflbm
-from cflbm import Solver
+from cflbm import Batch, Solver
 
 pytestmark = pytest.mark.gpu
 
@@ -154,6 +154,27 @@ def test_channel_reduced_precision_close_to_oracle(cuda, storage, compute, tol):
         assert rel_err(r["u"], o["u"]) < tol, (name, storage, compute)
         assert rel_err(r["v"], o["v"]) < 20 * tol, (name, storage, compute)
         assert rel_err(r["force"][:, 0], o["force"][:, 0]) < 10 * tol, (name, storage, compute)
+
+
+@pytest.mark.parametrize("storage,tol", [("fp32", 2e-5), ("fp16dev", 3e-3)])
+def test_wide_d2q9_grid_close_to_oracle(cuda, storage, tol):
+    """D2Q9 grids of 2^20 cells and more take the 48-register pair kernel; it
+    must agree with the oracle as the other FP32-collision forms do, and bit for
+    bit with the same channel advanced as a one-instance batch (same cell code,
+    other kernels)."""
+    case = dict(lattice=9, nx=1024, ny=1024, nz=1, tau0=0.03, u0=0.05, wall_y="freeslip",
+                geom="cylinder", cx=200, cy=512, diam=64)
+    steps = 20
+    o = oracle_channel(case, steps)
+    r = gpu_channel(case, steps, storage=storage, compute="fp32")
+    assert rel_err(r["u"], o["u"]) < tol
+    assert rel_err(r["v"], o["v"]) < 20 * tol
+    assert rel_err(r["force"][:, 0], o["force"][:, 0]) < 10 * tol
+    with Batch([dict(case, perturb_amp=1e-3, seed=1234, storage=storage, compute="fp32")],
+               graph_steps=8, autotune=False, tile_height=4, blocks_per_sm=0) as b:
+        b.step(steps)
+        b.synchronize()
+        assert np.array_equal(b.instance(0).get_f(), r["fpost"])
 
 
 def test_brinkman_porosity_matches_oracle(cuda):
