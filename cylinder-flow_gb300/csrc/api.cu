@@ -61,7 +61,7 @@ void free_handle(cflbm_handle *h) {
   if (h->cfg.device >= 0) cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
-                  h->d_links_bits, h->d_tile_slow, h->d_slow_tiles,
+                  h->d_links_bits, h->d_tile_slow, h->d_slow_tiles, h->d_tile_index,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
                   h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
   for (void *p : ptrs)
@@ -435,6 +435,11 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     if ((rc = dev_alloc_t(h, &h->d_tile_slow, flag.size()))) return rc;
     CK_CUDA(cudaMemcpyAsync(h->d_tile_slow, flag.data(), flag.size(), cudaMemcpyHostToDevice,
                             h->stream));
+    std::vector<int> index(flag.size(), -1);
+    for (size_t t = 0; t < list.size(); ++t) index[(size_t)list[t]] = (int)t;
+    if ((rc = dev_alloc_t(h, &h->d_tile_index, index.size()))) return rc;
+    CK_CUDA(cudaMemcpyAsync(h->d_tile_index, index.data(), index.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, h->stream));
     if ((rc = dev_alloc_t(h, &h->d_slow_tiles, list.size() + 1))) return rc;
     if ((rc = dev_alloc_t(h, &h->d_links_bits, tile_bits.size() + 32))) return rc;
     if (!list.empty()) {
@@ -576,6 +581,7 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
       1, std::min<long long>((h->n_slow + SWEEP_BY - 1) / SWEEP_BY, (long long)per_sm * h->sms));
   sa.tile_slow = h->d_tile_slow;
   sa.slow_tiles = h->d_slow_tiles;
+  sa.tile_index = h->d_tile_index;
   sa.links_bits = h->d_links_bits;
   sa.n_slow = h->n_slow;
   sa.partials = h->d_partials;
@@ -606,7 +612,9 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   fa.f_in = h->d_fin;
   const bool ref = h->cfg.profile != CFLBM_PROFILE_CHANNEL;
   if (!ref) {
-    const SweepArgs sa = channel_args(h, h->fA, h->fB, write_macros);
+    // u, v, w, p are formed on request (ensure_macros), not written every step.
+    (void)write_macros;
+    const SweepArgs sa = channel_args(h, h->fA, h->fB, false);
     if (h->timing && (trc = record_event(h, &ts0))) return trc;
     CK_CUDA(launch_sweep_channel(Q, st, h->cfg.compute, sa, h->stream, &h->fork));
     if (h->timing) {
@@ -615,6 +623,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
     }
     std::swap(h->fA, h->fB);
     ++h->steps_done;
+    h->macros_pending = true;
     return CFLBM_OK;
   }
   if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
@@ -724,9 +733,20 @@ int cflbm_synchronize(cflbm_handle *h) {
   return CFLBM_OK;
 }
 
+// Channel profile: forms u, v, w, p of the last step from the state that step
+// read (fB after the step; intact until the next step), once per step.
+static int ensure_macros(cflbm_handle *h) {
+  if (!h->macros_pending) return CFLBM_OK;
+  const SweepArgs sa = channel_args(h, h->fB, nullptr, true);
+  CK_CUDA(launch_macros_channel(h->Q, h->cfg.storage, h->cfg.compute, sa, h->stream));
+  h->macros_pending = false;
+  return CFLBM_OK;
+}
+
 int cflbm_macros(cflbm_handle *h, double *u, double *v, double *w, double *p) {
   if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
   CK_CUDA(cudaSetDevice(h->cfg.device));
+  if (int rc = ensure_macros(h)) return rc;
   const size_t N = (size_t)h->L.nx * h->L.ny * h->L.nz;
   double *dst[4] = {u, v, w, p};
   double *src[4] = {h->d_mu, h->d_mv, h->d_mw, h->d_mp};
@@ -739,6 +759,7 @@ int cflbm_macros(cflbm_handle *h, double *u, double *v, double *w, double *p) {
 int cflbm_macros_device(cflbm_handle *h, double *u, double *v, double *w, double *p) {
   if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
   CK_CUDA(cudaSetDevice(h->cfg.device));
+  if (int rc = ensure_macros(h)) return rc;
   const size_t N = (size_t)h->L.nx * h->L.ny * h->L.nz;
   double *dst[4] = {u, v, w, p};
   double *src[4] = {h->d_mu, h->d_mv, h->d_mw, h->d_mp};
@@ -846,6 +867,7 @@ int cflbm_set_f(cflbm_handle *h, const double *in, int64_t steps_done) {
   cudaFree(d);
   CK_CUDA(e);
   h->steps_done = steps_done;
+  h->macros_pending = false;
   long long st = steps_done;
   CK_CUDA(cudaMemcpy(h->d_step, &st, sizeof(st), cudaMemcpyHostToDevice));
   return CFLBM_OK;

@@ -463,6 +463,16 @@ cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a, 
 cudaError_t launch_sweep_channel_q27(int store, int compute, const SweepArgs &a, cudaStream_t s,
                                       const SweepFork *fk);
 
+cudaError_t launch_macros_channel_q9(int store, int compute, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_macros_channel_q27(int store, int compute, const SweepArgs &a,
+                                      cudaStream_t s);
+
+cudaError_t launch_macros_channel(int Q, int store, int compute, const SweepArgs &a,
+                                  cudaStream_t s) {
+  return Q == 9 ? launch_macros_channel_q9(store, compute, a, s)
+                : launch_macros_channel_q27(store, compute, a, s);
+}
+
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
                                  cudaStream_t s, const SweepFork *fk) {
   return Q == 9 ? launch_sweep_channel_q9(store, compute, a, s, fk)

@@ -22,6 +22,10 @@ struct cflbm_handle {
   unsigned *d_links_bits = nullptr;  // link bits of the tiles next to solids
   unsigned char *d_tile_slow = nullptr;  // per warp tile: needs the resolving kernel
   int *d_slow_tiles = nullptr;           // list of those tiles
+  int *d_tile_index = nullptr;           // per warp tile: position in that list or -1
+  // Channel profile: the steps do not write u, v, w, p; the fields of the last
+  // step are formed on request from the state it read (fB after the step).
+  bool macros_pending = false;
   int n_slow = 0;
   double f_in[27] = {0};        // inlet equilibrium (channel profile)
   int4 *d_links = nullptr;

@@ -68,6 +68,7 @@ struct SweepArgs {
   float f_in_f[27];      // the same in FP32 (FP32-arithmetic sweeps)
   const unsigned char *tile_slow;  // per warp tile (32 cells of a row): 1 = next to a solid
   const int *slow_tiles; // list of tiles next to solids (tile = (z*ny + y)*nxw + x/32)
+  const int *tile_index; // per warp tile: its position in slow_tiles, -1 if not listed
   int n_slow;            // length of the list
   const unsigned *links_bits;  // per listed tile, 32 cells: bit i = source of i is solid
   double *partials;      // 3 doubles per block of the resolving kernel
@@ -125,6 +126,9 @@ struct SweepFork {
   cudaStream_t side;
   cudaEvent_t fork, join;
 };
+// u, v, w, p of the step that read a.fa (channel profile), into a.mu..a.mp.
+cudaError_t launch_macros_channel(int Q, int store, int compute, const SweepArgs &a,
+                                  cudaStream_t s);
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
                                  cudaStream_t s, const SweepFork *fk = nullptr);
 // Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z

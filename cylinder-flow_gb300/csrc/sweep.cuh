@@ -155,23 +155,28 @@ __device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz
 
 // Macros out (when requested), Brinkman damping of the equilibrium velocity,
 // relaxation, store: the common tail of every sweep.
+// u, v, w and p = rho3 / 3 of one cell into the FP64 macroscopic fields.
+template <class A>
+__device__ __forceinline__ void store_macros(const SweepArgs &a, long long cell, A rho3, A ux,
+                                             A uy, A uz) {
+  if constexpr (sizeof(A) == 4) {
+    a.mu[cell] = f2d_bits(ux);
+    a.mv[cell] = f2d_bits(uy);
+    a.mw[cell] = f2d_bits(uz);
+    a.mp[cell] = f2d_bits(__fmul_rn(rho3, 1.0f / 3.0f));
+  } else {
+    a.mu[cell] = ux;
+    a.mv[cell] = uy;
+    a.mw[cell] = uz;
+    a.mp[cell] = __ddiv_rn(rho3, 3.0);
+  }
+}
+
 template <class L, class SF, class A, class E>
 __device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long long cell,
                                             bool store, E *__restrict__ fb, long long c,
                                             long long S, const SweepArgs &a) {
-  if (a.mu && store) {
-    if constexpr (sizeof(A) == 4) {
-      a.mu[cell] = f2d_bits(ux);
-      a.mv[cell] = f2d_bits(uy);
-      a.mw[cell] = f2d_bits(uz);
-      a.mp[cell] = f2d_bits(__fmul_rn(rho3, 1.0f / 3.0f));
-    } else {
-      a.mu[cell] = ux;
-      a.mv[cell] = uy;
-      a.mw[cell] = uz;
-      a.mp[cell] = __ddiv_rn(rho3, 3.0);
-    }
-  }
+  if (a.mu && store) store_macros<A>(a, cell, rho3, ux, uy, uz);
   if (a.alpha) {
     const A s = VA<A>::sub(A(1), static_cast<A>(a.alpha[cell]));
     ux = VA<A>::mul(ux, s);
@@ -578,6 +583,54 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
       }
     }
   }
+}
+
+// Macroscopic fields of the step that read a.fa, formed on request instead of
+// in every step: the step's pull (the resolved pull, which equals the plain one
+// away from faces and solids), its moments and its solid rule, one cell per
+// thread, written as the sweep writes them.  Reads the Q populations of every
+// cell once and writes 4 doubles per cell.
+template <int Q, class ST, class A>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY) macros_channel_kernel(const SweepArgs a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx, ny = a.L.ny;
+  const int lane = threadIdx.x;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y, z = blockIdx.z;
+  if (y >= ny) return;
+  const long long tile = ((long long)z * ny + y) * a.nxw + blockIdx.x;
+  const int t = a.tile_index[tile];
+  int x = blockIdx.x * SWEEP_BX + lane;
+  const bool valid = x < nx;
+  if (!valid) x = nx - 1;
+  const unsigned links = t >= 0 ? a.links_bits[(long long)t * SWEEP_BX + lane] : 0u;
+  const bool solid_here = t >= 0 && mask_solid(a.mask, a.nxw, ny, x, y, z);
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  A f[Q];
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        f[I] = pull_resolved<Q, ST, A, I>(fa, c, S, x, y, z, links, a);
+      },
+      std::make_integer_sequence<int, Q>{});
+  A rho3, ux, uy, uz;
+  moments<L, A, SF>(f, rho3, ux, uy, uz);
+  if (solid_here) {
+    rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
+  }
+  if (valid) store_macros<A>(a, ((long long)z * ny + y) * nx + x, rho3, ux, uy, uz);
+}
+
+template <int Q, class ST, class A>
+cudaError_t launch_macros_channel_t(const SweepArgs &a, cudaStream_t s) {
+  dim3 block(SWEEP_BX, SWEEP_BY, 1);
+  dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
+  macros_channel_kernel<Q, ST, A><<<grid, block, 0, s>>>(a);
+  count_launch();
+  return cudaGetLastError();
 }
 
 // The interior launch: FP32 collision on FP32 or FP16 storage takes the packed

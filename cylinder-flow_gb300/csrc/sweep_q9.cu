@@ -38,4 +38,22 @@ cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a,
   return cudaErrorInvalidValue;
 }
 
+cudaError_t launch_macros_channel_q9(int store, int compute, const SweepArgs &a,
+                                      cudaStream_t s) {
+  if (compute == COMPUTE_F64) {
+    switch (store) {
+      case STORE_F64: return launch_macros_channel_t<9, double, double>(a, s);
+      case STORE_F32: return launch_macros_channel_t<9, float, double>(a, s);
+      case STORE_F16: return launch_macros_channel_t<9, F16Dev, double>(a, s);
+    }
+  } else {
+    switch (store) {
+      case STORE_F64: return launch_macros_channel_t<9, double, float>(a, s);
+      case STORE_F32: return launch_macros_channel_t<9, float, float>(a, s);
+      case STORE_F16: return launch_macros_channel_t<9, F16Dev, float>(a, s);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace cflbm

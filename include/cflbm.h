@@ -126,7 +126,10 @@ int cflbm_synchronize(cflbm_handle *h);
 /* Macroscopic fields after the last step: u, v, w, p over the interior, x
  * fastest, as LBM::Update leaves them ("3D.../lbm.cpp:374-417": p = sum f/3,
  * u = sum f e, zero in solids, reference-profile inlet/outlet overrides).
- * Any pointer may be NULL.  Host pointers; synchronises. */
+ * Any pointer may be NULL.  Host pointers; synchronises.  CHANNEL profile: the
+ * steps do not write these fields; the first call after a step forms them from
+ * the state that step read (one read of the populations, bit-identical to
+ * forming them inside the step). */
 int cflbm_macros(cflbm_handle *h, double *u, double *v, double *w, double *p);
 
 /* Same, into device pointers (no synchronisation; ordered on the handle's
