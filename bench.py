@@ -12,8 +12,10 @@ is measured and reported alongside as "fp64_arith").
 One step = one time step of the whole grid (boundary kernel + fused sweep).
 `value` = interior cells x timed steps / device time (MLUPS), inputs resident;
 `e2e` = the same metric through the C ABI end to end: create the handle from
-host buffers, step, read every step's force (Cd, Cl) back to the host as the
-reference's test.dat loop does, and read the final u, v, w, p fields back.
+host buffers (page-locked solid mask), step, read every step's force back to
+page-locked host memory as the reference's test.dat loop does (queued behind the
+step, so the next step is queued before it arrives), and read the final u, v, w,
+p fields back.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -240,21 +242,28 @@ def run_gb300(args):
     solid = np.zeros((NZ, NY, NX), np.uint8)
     yy, xx = np.mgrid[0:NY, 0:NX]
     solid[:, ((xx - 128.0) ** 2 + (yy - 64.0) ** 2) <= (D / 2) ** 2] = 1
+    solid_pinned = torch.from_numpy(solid).pin_memory()
     pinned = [torch.empty((NZ, NY, NX), dtype=torch.float64).pin_memory() for _ in range(4)]
+    forces_pinned = torch.zeros((e2e_steps, 3), dtype=torch.float64).pin_memory()
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     wl = dict(WORKLOAD)
     wl["geom"] = "none"
-    with cflbm.Solver(device=local, storage="fp64", compute="fp32", solid=solid, **wl) as s:
-        for _ in range(e2e_steps):
+    with cflbm.Solver(device=local, storage="fp64", compute="fp32", solid=solid_pinned.numpy(),
+                      **wl) as s:
+        for k in range(e2e_steps):
             s.step(1)
-            s.forces()  # per-step Cd/Cl read back (reference: test.dat every step)
+            # every step's force read back to the host (the reference writes
+            # Cd/Cl to test.dat every step), queued behind the step
+            s.forces_async(forces_pinned[k].data_ptr())
         outs = [t.numpy() for t in pinned]
         cflbm._lib.check(cflbm._lib.lib.cflbm_macros(
             s._h, *[o.ctypes.data_as(cflbm.solver.ctypes.POINTER(cflbm.solver.ctypes.c_double))
-                    for o in outs]), "cflbm_macros")
+                    for o in outs]), "cflbm_macros")  # synchronises
+        hist_last = s.force_history()[-1]
     t1 = time.perf_counter()
+    forces_ok = bool(np.array_equal(forces_pinned[-1].numpy(), hist_last))
     e2e_s = max_over_ranks(t1 - t0, world)
     e2e_value = world * CELLS * e2e_steps / e2e_s / 1e6
     h2d = solid.nbytes / e2e_steps
@@ -283,7 +292,7 @@ def run_gb300(args):
                      "sweep_us": round(sweep_s * 1e6, 2),
                      "boundary_us": round(1e3 * bd_ms / max(n_bd, 1), 2)},
         "e2e": {"value": round(e2e_value, 2), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps, "forces_read_back": forces_ok},
         "gpu_launches": gpu_launches,
         "clocks": clk.summary(),
         "forms": extra,

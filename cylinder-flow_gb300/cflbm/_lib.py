@@ -88,6 +88,7 @@ SIGNATURES = {
     "cflbm_macros_device": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "cflbm_forces": ([ctypes.c_void_p, _dp, _dp], ctypes.c_int),
+    "cflbm_forces_async": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "cflbm_force_history": ([ctypes.c_void_p, _dp, ctypes.c_int64,
                              ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cflbm_mass": ([ctypes.c_void_p, _dp, _dp], ctypes.c_int),

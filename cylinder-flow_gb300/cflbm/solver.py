@@ -102,6 +102,13 @@ class Solver:
         C.check(C.lib.cflbm_forces(self._h, _ptr(f), _ptr(c)), "cflbm_forces")
         return f, c
 
+    def forces_async(self, ptr: int):
+        """Queue a copy of the last step's (Fx, Fy, Fz) to host address `ptr`
+        (3 doubles, page-locked for the copy to be asynchronous); valid after
+        synchronize()."""
+        C.check(C.lib.cflbm_forces_async(self._h, ctypes.c_void_p(int(ptr))),
+                "cflbm_forces_async")
+
     def force_history(self, max_steps: int | None = None):
         if max_steps is None:
             max_steps = self.info().steps_done

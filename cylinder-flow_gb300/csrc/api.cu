@@ -797,6 +797,20 @@ int cflbm_forces(cflbm_handle *h, double fxyz[3], double cd_cl[2]) {
   return CFLBM_OK;
 }
 
+int cflbm_forces_async(cflbm_handle *h, double fxyz[3]) {
+  if (!h || !fxyz) return fail(CFLBM_E_INVALID, "bad arguments");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  if (h->steps_done == 0) {  // no step yet: zero, once earlier copies into fxyz are done
+    CK_CUDA(cudaStreamSynchronize(h->stream));
+    fxyz[0] = fxyz[1] = fxyz[2] = 0.0;
+    return CFLBM_OK;
+  }
+  const long long slot = (h->steps_done - 1) % h->hist_cap;
+  CK_CUDA(cudaMemcpyAsync(fxyz, h->d_hist + 3 * slot, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                          h->stream));
+  return CFLBM_OK;
+}
+
 int cflbm_force_history(cflbm_handle *h, double *out, int64_t max_steps, int64_t *n_out) {
   if (!h || !out || max_steps < 0) return fail(CFLBM_E_INVALID, "bad arguments");
   CK_CUDA(cudaSetDevice(h->cfg.device));

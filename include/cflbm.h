@@ -143,6 +143,13 @@ int cflbm_macros_device(cflbm_handle *h, double *d_u, double *d_v, double *d_w, 
  * Either pointer may be NULL.  Synchronises. */
 int cflbm_forces(cflbm_handle *h, double fxyz[3], double cd_cl[2]);
 
+/* The same (Fx, Fy, Fz) of the last step queued on the handle's stream as an
+ * asynchronous device-to-host copy into fxyz (page-locked memory makes it
+ * asynchronous); valid after cflbm_synchronize.  Lets a caller that reads every
+ * step's force (the reference writes test.dat every step) queue the next step
+ * before that force has arrived. */
+int cflbm_forces_async(cflbm_handle *h, double fxyz[3]);
+
 /* Per-step force history (Fx, Fy, Fz per step, oldest first) of the last
  * min(steps_done, capacity) steps.  Writes up to max_steps rows into out
  * (3*max_steps doubles) and the row count into *n_out.  Synchronises. */

@@ -272,3 +272,22 @@ def test_launches_are_counted(cuda):
         s.step(5)
         s.synchronize()
     assert cflbm.launch_count() - n0 >= 2 * 5  # fast + resolving sweep per step
+
+
+def test_forces_async_matches_forces(cuda):
+    """cflbm_forces_async queues the same (Fx, Fy, Fz) that cflbm_forces returns,
+    step by step, without synchronising."""
+    import torch
+    case = CHANNEL_CASES["d2q9_cyl_freeslip"]
+    out = torch.full((6, 3), -1.0, dtype=torch.float64).pin_memory()
+    with Solver(perturb_amp=1e-3, seed=1234, **case) as s:
+        s.forces_async(out[0].data_ptr())  # before any step: zero
+        for k in range(1, 6):
+            s.step(1)
+            s.forces_async(out[k].data_ptr())
+        s.synchronize()
+        hist = s.force_history()
+        f, _ = s.forces()
+    assert np.array_equal(out[0].numpy(), np.zeros(3))
+    assert np.array_equal(out[1:].numpy(), hist[:5])
+    assert np.array_equal(out[5].numpy(), f)
