@@ -86,11 +86,10 @@ int store_size(int storage) {
 std::vector<uint32_t> pack_mask(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
                                 int nxw) {
   std::vector<uint32_t> w((size_t)nxw * ny * nz, 0u);
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < ny; ++y)
-      for (int x = 0; x < nx; ++x)
-        if (solid[((size_t)z * ny + y) * nx + x])
-          w[((size_t)z * ny + y) * nxw + (x >> 5)] |= (1u << (x & 31));
+  host_parallel_rows((long long)ny * nz, [&](long long r) {
+    for (int x = 0; x < nx; ++x)
+      if (solid[(size_t)r * nx + x]) w[(size_t)r * nxw + (x >> 5)] |= (1u << (x & 31));
+  });
   return w;
 }
 
@@ -98,37 +97,33 @@ template <int Q>
 void build_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
                  std::vector<int4> &links, long long &n_solid) {
   using L = Lat<Q>;
+  // Rows in parallel, then concatenated in row order: the list order (z, y, x,
+  // direction) fixes the order of the force sums over links.
+  const long long rows = (long long)ny * nz;
+  std::vector<std::vector<int4>> per(rows);
+  std::vector<long long> nsol(rows, 0);
+  host_parallel_rows(rows, [&](long long r) {
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    for (int x = 0; x < nx; ++x) {
+      if (!solid[(size_t)r * nx + x]) continue;
+      ++nsol[r];
+      for (int k = 1; k < Q; ++k) {
+        const int X = x + L::ex(k), Y = y + L::ey(k), Z = z + L::ez(k);
+        if (X < 0 || X >= nx || Y < 0 || Y >= ny || Z < 0 || Z >= nz) continue;
+        if (solid[((size_t)Z * ny + Y) * nx + X]) continue;
+        per[r].push_back(make_int4(x, y, z, k));
+      }
+    }
+  });
   links.clear();
   n_solid = 0;
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < ny; ++y)
-      for (int x = 0; x < nx; ++x) {
-        if (!solid[((size_t)z * ny + y) * nx + x]) continue;
-        ++n_solid;
-        for (int k = 1; k < Q; ++k) {
-          const int X = x + L::ex(k), Y = y + L::ey(k), Z = z + L::ez(k);
-          if (X < 0 || X >= nx || Y < 0 || Y >= ny || Z < 0 || Z >= nz) continue;
-          if (solid[((size_t)Z * ny + Y) * nx + X]) continue;
-          links.push_back(make_int4(x, y, z, k));
-        }
-      }
-}
-
-// Run body(r) for r in [0, n) on the host's cores (rows are independent).
-template <class F>
-void host_parallel_rows(long long n, F body) {
-  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-  const long long nt = std::min<long long>(hw, std::max<long long>(1, n / 64));
-  if (nt <= 1) {
-    for (long long r = 0; r < n; ++r) body(r);
-    return;
+  size_t total = 0;
+  for (long long r = 0; r < rows; ++r) total += per[r].size();
+  links.reserve(total);
+  for (long long r = 0; r < rows; ++r) {
+    links.insert(links.end(), per[r].begin(), per[r].end());
+    n_solid += nsol[r];
   }
-  std::vector<std::thread> pool;
-  for (long long t = 0; t < nt; ++t)
-    pool.emplace_back([=, &body] {
-      for (long long r = t; r < n; r += nt) body(r);
-    });
-  for (auto &th : pool) th.join();
 }
 
 // Channel-profile solid links: bit i of cell X is set when the source of
@@ -204,26 +199,36 @@ std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
                                        int nz, int nxw, std::vector<int> &list,
                                        std::vector<uint32_t> &tile_bits) {
   std::vector<unsigned char> flag((size_t)nxw * ny * nz, 0);
-  list.clear();
-  tile_bits.clear();
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < ny; ++y)
-      for (int w = 0; w < nxw; ++w) {
-        // Rows on a y or z face always need the resolving pull.
-        bool any = y == 0 || y == ny - 1 || (nz > 1 && (z == 0 || z == nz - 1));
-        for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !any; ++x) {
-          const size_t n = ((size_t)z * ny + y) * nx + x;
-          any = solid[n] || bits[n];
-        }
-        if (!any) continue;
-        const size_t t = ((size_t)z * ny + y) * nxw + w;
-        flag[t] = 1;
-        list.push_back((int)t);
-        for (int l = 0; l < 32; ++l) {
-          const int x = w * 32 + l;
-          tile_bits.push_back(x < nx ? bits[((size_t)z * ny + y) * nx + x] : 0u);
-        }
+  // Rows in parallel, concatenated in row order (the list is ordered by tile).
+  const long long rows = (long long)ny * nz;
+  std::vector<std::vector<int>> per(rows);
+  host_parallel_rows(rows, [&](long long r) {
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    for (int w = 0; w < nxw; ++w) {
+      // Rows on a y or z face always need the resolving pull.
+      bool any = y == 0 || y == ny - 1 || (nz > 1 && (z == 0 || z == nz - 1));
+      for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !any; ++x) {
+        const size_t n = (size_t)r * nx + x;
+        any = solid[n] || bits[n];
       }
+      if (!any) continue;
+      const size_t t = (size_t)r * nxw + w;
+      flag[t] = 1;
+      per[r].push_back((int)t);
+    }
+  });
+  list.clear();
+  for (long long r = 0; r < rows; ++r) list.insert(list.end(), per[r].begin(), per[r].end());
+  tile_bits.assign(list.size() * 32, 0u);
+  host_parallel_rows((long long)list.size(), [&](long long k) {
+    const long long t = list[k];
+    const long long r = t / nxw;
+    const int w = (int)(t % nxw);
+    for (int l = 0; l < 32; ++l) {
+      const int x = w * 32 + l;
+      tile_bits[(size_t)k * 32 + l] = x < nx ? bits[(size_t)r * nx + x] : 0u;
+    }
+  });
   return flag;
 }
 
@@ -385,10 +390,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     solid = ref.solid;
     h->area = ref.area;
   } else {
-    channel_mask(h->cfg, solid);
-    if (cfg->solid) {
-      for (size_t n = 0; n < solid.size(); ++n) solid[n] = cfg->solid[n] ? 1 : 0;
-    }
+    channel_mask(*cfg, solid);  // cfg->solid (nonzero = solid) when given, else the geometry
     h->area = channel_area(h->cfg);
   }
   std::vector<int4> links;

@@ -1,7 +1,9 @@
 // Internal handle state and host-side helpers shared by the C ABI sources.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 #include <cuda_runtime.h>
 #include "../../include/cflbm.h"
@@ -83,5 +85,22 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
 // Tecplot binary writer (tecplot.cpp).
 int write_tecplot(const char *path, int dim, int nx, int ny, int nz, const double *u,
                   const double *v, const double *w, const double *p, int n);
+
+// Run body(r) for r in [0, n) on the host's cores (rows are independent).
+template <class F>
+void host_parallel_rows(long long n, F body) {
+  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const long long nt = std::min<long long>(hw, std::max<long long>(1, n / 64));
+  if (nt <= 1) {
+    for (long long r = 0; r < n; ++r) body(r);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (long long t = 0; t < nt; ++t)
+    pool.emplace_back([=, &body] {
+      for (long long r = t; r < n; r += nt) body(r);
+    });
+  for (auto &th : pool) th.join();
+}
 
 }  // namespace cflbm

@@ -95,16 +95,18 @@ void channel_mask(const cflbm_config &c, std::vector<uint8_t> &solid) {
     for (size_t n = 0; n < N; ++n) solid[n] = c.solid[n] ? 1 : 0;
     return;
   }
+  if (c.geom != CFLBM_GEOM_CYLINDER && c.geom != CFLBM_GEOM_SPHERE) return;
   const double r2 = 0.25 * c.diam * c.diam;
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < c.ny; ++y)
-      for (int x = 0; x < c.nx; ++x) {
-        const double dx = x - c.cx, dy = y - c.cy, dz = z - c.cz;
-        bool s = false;
-        if (c.geom == CFLBM_GEOM_CYLINDER) s = dx * dx + dy * dy <= r2;
-        else if (c.geom == CFLBM_GEOM_SPHERE) s = dx * dx + dy * dy + dz * dz <= r2;
-        solid[((size_t)z * c.ny + y) * c.nx + x] = s ? 1 : 0;
-      }
+  host_parallel_rows((long long)c.ny * nz, [&](long long r) {
+    const int y = (int)(r % c.ny), z = (int)(r / c.ny);
+    for (int x = 0; x < c.nx; ++x) {
+      const double dx = x - c.cx, dy = y - c.cy, dz = z - c.cz;
+      bool s = false;
+      if (c.geom == CFLBM_GEOM_CYLINDER) s = dx * dx + dy * dy <= r2;
+      else s = dx * dx + dy * dy + dz * dz <= r2;
+      solid[(size_t)r * c.nx + x] = s ? 1 : 0;
+    }
+  });
 }
 
 double channel_area(const cflbm_config &c) {
