@@ -62,6 +62,7 @@ void free_handle(cflbm_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
                   h->d_links_bits, h->d_tile_slow, h->d_slow_tiles, h->d_tile_index,
+                  h->d_face_off, h->d_face_bb,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
                   h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
   for (void *p : ptrs)
@@ -190,6 +191,43 @@ std::vector<uint32_t> channel_links(const std::vector<uint8_t> &solid, int nx, i
   return bits;
 }
 
+// Pull tables of the listed tiles, one row per face state (bit 0: y = 0, bit 1:
+// y = ny-1, bit 2: z = 0, bit 3: z = nz-1).  For every direction i: the source
+// offset relative to the cell, population slot included, after the sweep's y/z
+// face rules (periodic wrap; free-slip mirror: the same row and the mirrored
+// population), and bit i of bb when a no-slip face bounces i back.  These are
+// pull_resolved's face rules resolved once per state instead of per cell; the
+// x rules (inlet, zero-gradient outlet) and solid links stay per cell.
+template <int Q>
+void face_tables(const Layout &Ly, int wall_y, int wall_z, std::vector<long long> &off,
+                 std::vector<uint32_t> &bb) {
+  using L = Lat<Q>;
+  off.assign(16 * (size_t)Q, 0);
+  bb.assign(16, 0u);
+  for (int st = 0; st < 16; ++st)
+    for (int i = 1; i < Q; ++i) {
+      const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+      long long src = -Ly.off(ex, ey, ez);
+      bool my = false, mz = false, b = false;
+      if (ez != 0) {
+        const bool out = ez > 0 ? (st & 4) : (st & 8);
+        if (out && wall_z == CFLBM_WALL_PERIODIC) src += (ez > 0 ? 1LL : -1LL) * Ly.nz * Ly.zs;
+        if (out && wall_z == CFLBM_WALL_FREESLIP) { mz = true; src += (long long)ez * Ly.zs; }
+        if (out && wall_z == CFLBM_WALL_NOSLIP) b = true;
+      }
+      if (ey != 0) {
+        const bool out = !b && (ey > 0 ? (st & 1) : (st & 2));
+        if (out && wall_y == CFLBM_WALL_PERIODIC) src += (ey > 0 ? 1LL : -1LL) * Ly.ny * Ly.rs;
+        if (out && wall_y == CFLBM_WALL_FREESLIP) { my = true; src += (long long)ey * Ly.rs; }
+        if (out && wall_y == CFLBM_WALL_NOSLIP) b = true;
+      }
+      const int j = my ? (mz ? mirror<L>(mirror<L>(i, 1), 2) : mirror<L>(i, 1))
+                       : (mz ? mirror<L>(i, 2) : i);
+      off[(size_t)st * Q + i] = (long long)j * Ly.S + src;
+      if (b) bb[st] |= 1u << i;
+    }
+}
+
 // Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) holding a
 // solid cell or a cell with solid links: the second channel launch handles
 // them.  Fills the list and the 32 link words of every listed tile; returns the
@@ -226,7 +264,8 @@ std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
     const int w = (int)(t % nxw);
     for (int l = 0; l < 32; ++l) {
       const int x = w * 32 + l;
-      tile_bits[(size_t)k * 32 + l] = x < nx ? bits[(size_t)r * nx + x] : 0u;
+      tile_bits[(size_t)k * 32 + l] =
+          x < nx ? bits[(size_t)r * nx + x] | (solid[(size_t)r * nx + x] ? 1u << 31 : 0u) : 0u;
     }
   });
   return flag;
@@ -442,6 +481,16 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     if ((rc = dev_alloc_t(h, &h->d_tile_index, index.size()))) return rc;
     CK_CUDA(cudaMemcpyAsync(h->d_tile_index, index.data(), index.size() * sizeof(int),
                             cudaMemcpyHostToDevice, h->stream));
+    std::vector<long long> foff;
+    std::vector<uint32_t> fbb;
+    if (d3) face_tables<27>(L, cfg->wall_y, cfg->wall_z, foff, fbb);
+    else face_tables<9>(L, cfg->wall_y, cfg->wall_z, foff, fbb);
+    if ((rc = dev_alloc_t(h, &h->d_face_off, foff.size()))) return rc;
+    if ((rc = dev_alloc_t(h, &h->d_face_bb, fbb.size()))) return rc;
+    CK_CUDA(cudaMemcpyAsync(h->d_face_off, foff.data(), foff.size() * sizeof(long long),
+                            cudaMemcpyHostToDevice, h->stream));
+    CK_CUDA(cudaMemcpyAsync(h->d_face_bb, fbb.data(), fbb.size() * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, h->stream));
     if ((rc = dev_alloc_t(h, &h->d_slow_tiles, list.size() + 1))) return rc;
     if ((rc = dev_alloc_t(h, &h->d_links_bits, tile_bits.size() + 32))) return rc;
     if (!list.empty()) {
@@ -573,17 +622,18 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
     sa.f_in[i] = h->f_in[i] * sc;
     sa.f_in_f[i] = (float)(h->f_in[i] * sc);
   }
-  // Persistent grid of the listed-tile launch, in blocks per SM: the fewer, the
-  // more of each SM the interior launch keeps; too few and the listed tiles
-  // outlast it.  Measured on the D3Q27 512x128x128 bench step: FP64 storage
-  // 0.973 / 0.960 / 0.949 of the copy peak at 1 / 2 / 3 per SM, FP32 storage
-  // 0.850 / 0.883 / 0.880, FP16 storage flat (0.613 / 0.608 / 0.600).
-  const int per_sm = h->cfg.storage == CFLBM_STORE_FP32 ? 2 : 1;
+  // Persistent grid of the force launch beside the sweep: one block per SM
+  // (measured on the D3Q27 512x128x128 bench step: 1 / 2 / 4 per SM give FP32
+  // storage 31.07 / 30.97 / 30.74, FP16 41.72 / 41.48 / 41.12, FP64 15.80 /
+  // 15.73 / 15.67 G cell updates/s).
+  const int per_sm = 1;
   sa.bnd_blocks = (int)std::max<long long>(
       1, std::min<long long>((h->n_slow + SWEEP_BY - 1) / SWEEP_BY, (long long)per_sm * h->sms));
   sa.tile_slow = h->d_tile_slow;
   sa.slow_tiles = h->d_slow_tiles;
   sa.tile_index = h->d_tile_index;
+  sa.face_off = h->d_face_off;
+  sa.face_bb = h->d_face_bb;
   sa.links_bits = h->d_links_bits;
   sa.n_slow = h->n_slow;
   sa.partials = h->d_partials;

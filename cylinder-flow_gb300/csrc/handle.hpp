@@ -25,6 +25,8 @@ struct cflbm_handle {
   unsigned char *d_tile_slow = nullptr;  // per warp tile: needs the resolving kernel
   int *d_slow_tiles = nullptr;           // list of those tiles
   int *d_tile_index = nullptr;           // per warp tile: position in that list or -1
+  long long *d_face_off = nullptr;       // listed-tile pull offsets per face state
+  unsigned *d_face_bb = nullptr;         // no-slip face bounce-back bits per face state
   // Channel profile: the steps do not write u, v, w, p; the fields of the last
   // step are formed on request from the state it read (fB after the step).
   bool macros_pending = false;

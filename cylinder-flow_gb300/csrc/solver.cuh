@@ -70,7 +70,10 @@ struct SweepArgs {
   const int *slow_tiles; // list of tiles next to solids (tile = (z*ny + y)*nxw + x/32)
   const int *tile_index; // per warp tile: its position in slow_tiles, -1 if not listed
   int n_slow;            // length of the list
-  const unsigned *links_bits;  // per listed tile, 32 cells: bit i = source of i is solid
+  const unsigned *links_bits;  // per listed tile, 32 cells: bit i = source of i is solid,
+                               // bit 31 = the cell is solid
+  const long long *face_off;   // [16][Q] listed-tile pull offsets per face state
+  const unsigned *face_bb;     // [16] directions bouncing back at a no-slip face
   double *partials;      // 3 doubles per block of the resolving kernel
   unsigned int *counter; // finished force blocks (self-resetting)
   double *hist;          // force history, 3 doubles per step

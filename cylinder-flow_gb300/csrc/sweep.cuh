@@ -14,18 +14,23 @@
 // population is a pure shift, so every element of A is read exactly once) plus
 // 1/8 byte of solid mask.
 //
-// Three kernels:
+// Kernels:
 //   sweep_kernel          -- reference profiles: ghost layers and solid cells
 //                            were filled by the boundary passes, so the pull is
 //                            plain; applies the reference's inlet/outlet
 //                            overrides of Update.
-//   sweep_channel_kernel  -- channel profile, in two launches: <false> over
-//                            every warp tile away from the y/z faces and from
-//                            solids (plain pulls), <true> over the listed face-row
-//                            and solid-adjacent tiles (resolved pulls, per-cell
-//                            link bits, body-force reduction).  Keeping the
-//                            boundary code out of the first launch holds it at
-//                            64 registers with all loads independent.
+//   sweep_channel2_kernel -- channel profile, FP32 collision on FP32/FP16
+//   sweep_channel_kernel     storage (two cells per thread, packed FP32x2) and
+//                            the other forms (one cell per thread), over every
+//                            warp tile: unlisted tiles pull plainly; listed
+//                            tiles (y/z face rows, tiles next to solids) take
+//                            their face rules from per-face-state offset tables
+//                            and their solid links from per-cell link words, so
+//                            the branch adds one select per direction, not the
+//                            per-cell wall logic of pull_resolved.
+//   channel_force_kernel  -- beside the sweep on a second stream: the body force
+//                            from the populations the sweep bounces back.
+//   macros_channel_kernel -- u, v, w, p on request.
 #pragma once
 #include <type_traits>
 #include <utility>
@@ -320,6 +325,37 @@ __device__ __forceinline__ A pull_resolved(const typename Store<ST>::elem *__res
   }
 }
 
+// Face state of a row: bit 0 y = 0, bit 1 y = ny-1, bit 2 z = 0, bit 3 z = nz-1.
+__device__ __forceinline__ int face_state(int y, int z, int ny, int nz) {
+  return (y == 0 ? 1 : 0) | (y == ny - 1 ? 2 : 0) | (z == 0 ? 4 : 0) | (z == nz - 1 ? 8 : 0);
+}
+
+// Post-stream population I of a cell of a listed tile, from the face-state
+// tables (off = a.face_off[state * Q + I], wbb = the no-slip face bit of I): the
+// same source as pull_resolved.  Solid link (bit I of `links`) or no-slip face:
+// halfway bounce-back f*_{opp(I)}(X); otherwise the table's source with the
+// per-cell x rules (inlet equilibrium at x = 0, zero gradient at x = nx-1).  A
+// mirrored population has the same |e| and e_x as I, so I's storage scale and
+// inlet value apply.
+template <int Q, class ST, class A, int I>
+__device__ __forceinline__ A pull_listed(const typename Store<ST>::elem *__restrict__ fa,
+                                         long long c, long long S, int x, long long off,
+                                         bool wbb, unsigned links, const SweepArgs &a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using Dd = DirC<Q, I>;
+  if constexpr (I == 0) {
+    return SF::template load<A, L>(fa + c, 0);
+  } else {
+    const bool bb = wbb || ((links >> I) & 1u);
+    long long src = c + off;
+    if constexpr (Dd::ex < 0) src += (x == a.L.nx - 1) ? Dd::ex : 0;  // zero gradient
+    A v = SF::template load<A, L>(fa + (bb ? (long long)Dd::opp * S + c : src), I);
+    if constexpr (Dd::ex > 0) v = (!bb && x == 0) ? inlet_pop<A>(a, I) : v;
+    return v;
+  }
+}
+
 // Force of one cell's solid bounce-backs, summed in the arithmetic type (at most
 // Q - 1 terms): each adds 2 f*_{opp(I)}(X) e_{opp(I)} = -2 v_I e_I (v_I in
 // storage units, scale of I).
@@ -345,7 +381,8 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
 // owns cells x and x + 32, whose loads and stores share their address (the
 // second is an immediate 32 elements further).  Moments and BGK run once on
 // float2 values (FADD2/FMUL2/FFMA2), halving the arithmetic instructions of
-// the issue-bound FP32-collision forms.  Listed tiles are skipped per half.
+// the issue-bound FP32-collision forms.  A pair holding a listed tile pulls
+// through pull_pair_listed (face-state tables and link words).
 template <int Q, class ST, int I>
 __device__ __forceinline__ float2 pull_pair(const typename Store<ST>::elem *__restrict__ p,
                                            const typename Store<ST>::elem *__restrict__ pm0,
@@ -368,11 +405,44 @@ __device__ __forceinline__ float2 pull_pair(const typename Store<ST>::elem *__re
   return make_float2(v0, v1);
 }
 
+// The pair pull of a listed tile pair: pull_listed for cells x0 and x0 + 32
+// (l0 / l1 their link words), both loads issued.
+template <int Q, class ST, int I>
+__device__ __forceinline__ float2 pull_pair_listed(const typename Store<ST>::elem *__restrict__ p,
+                                                   long long S, long long off, bool wbb,
+                                                   unsigned l0, unsigned l1, bool act1,
+                                                   bool out0, bool out1, bool inlet0,
+                                                   const SweepArgs &a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using Dd = DirC<Q, I>;
+  if constexpr (I == 0) {
+    return make_float2(SF::template load<float, L>(p, 0),
+                       act1 ? SF::template load<float, L>(p + 32, 0) : 0.0f);
+  } else {
+    const bool bb0 = wbb || ((l0 >> I) & 1u), bb1 = wbb || ((l1 >> I) & 1u);
+    long long s0 = off, s1 = off + 32;
+    if constexpr (Dd::ex < 0) {  // zero gradient at the outlet column
+      s0 += out0 ? Dd::ex : 0;
+      s1 += out1 ? Dd::ex : 0;
+    }
+    constexpr long long OS = Dd::opp;
+    float v0 = SF::template load<float, L>(p + (bb0 ? OS * S : s0), I);
+    const float v1 = act1 ? SF::template load<float, L>(p + (bb1 ? OS * S + 32 : s1), I) : 0.0f;
+    if constexpr (Dd::ex > 0) v0 = (!bb0 && inlet0) ? a.f_in_f[I] : v0;
+    return make_float2(v0, v1);
+  }
+}
+
 // Cells x0 and x0 + 32 of row (y, z) (x0 = 32 * even warp tile + lane); act0 /
 // act1: the two warp tiles are unlisted (warp-uniform).
-template <int Q, class ST>
+// LISTED: the pair holds a listed tile; both cells pull through the face-state
+// tables and their link words l0 / l1 (bit 31: solid cell), act0 = true and
+// act1 = the second tile exists.
+template <int Q, class ST, bool LISTED = false>
 __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y, int z,
-                                               bool act0, bool act1) {
+                                               bool act0, bool act1, unsigned l0 = 0u,
+                                               unsigned l1 = 0u) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
@@ -388,14 +458,31 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
   const E *__restrict__ pm1 = p + 32 - (x1 == nx - 1 ? 1 : 0);
   const bool inlet0 = x0 == 0;
   float2 f[Q];
-  static_for(
-      [&](auto ic) {
-        constexpr int I = decltype(ic)::value;
-        f[I] = pull_pair<Q, ST, I>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1, inlet0, a);
-      },
-      std::make_integer_sequence<int, Q>{});
+  if constexpr (LISTED) {
+    const int st = face_state(y, z, ny, a.L.nz);
+    const long long *__restrict__ offs = a.face_off + st * Q;
+    const unsigned wbb = a.face_bb[st];
+    static_for(
+        [&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          f[I] = pull_pair_listed<Q, ST, I>(p, S, offs[I], (wbb >> I) & 1u, l0, l1, act1,
+                                            x0 == nx - 1, x1 == nx - 1, inlet0, a);
+        },
+        std::make_integer_sequence<int, Q>{});
+  } else {
+    static_for(
+        [&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          f[I] = pull_pair<Q, ST, I>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1, inlet0, a);
+        },
+        std::make_integer_sequence<int, Q>{});
+  }
   float2 rho3, ux, uy, uz;
   moments<L, float2, SF>(f, rho3, ux, uy, uz);
+  if constexpr (LISTED) {  // solid cells: p = u = 0
+    if (l0 >> 31) { rho3.x = 0.0f; ux.x = 0.0f; uy.x = 0.0f; uz.x = 0.0f; }
+    if (l1 >> 31) { rho3.y = 0.0f; ux.y = 0.0f; uy.y = 0.0f; uz.y = 0.0f; }
+  }
   const long long cell0 = ((long long)z * ny + y) * nx + x0;
   if (a.mu) {
     if (st0) {
@@ -435,154 +522,186 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
   if (y >= ny) return;
   const int w0 = 2 * blockIdx.x;
   const long long trow = ((long long)z * ny + y) * a.nxw;
-  const bool act0 = !a.tile_slow[trow + w0];
-  const bool act1 = w0 + 1 < a.nxw && !a.tile_slow[trow + w0 + 1];
-  if (!act0 && !act1) return;  // whole warp
-  channel2_cells<Q, ST>(a, 32 * w0 + threadIdx.x, y, z, act0, act1);
+  const bool has1 = w0 + 1 < a.nxw;
+  const int t0 = a.tile_index[trow + w0];
+  const int t1 = has1 ? a.tile_index[trow + w0 + 1] : -1;
+  const int x0 = 32 * w0 + threadIdx.x;
+  if (t0 < 0 && t1 < 0) {  // warp-uniform
+    channel2_cells<Q, ST>(a, x0, y, z, true, has1);
+  } else {
+    const unsigned l0 = t0 >= 0 ? a.links_bits[(long long)t0 * SWEEP_BX + threadIdx.x] : 0u;
+    const unsigned l1 = t1 >= 0 ? a.links_bits[(long long)t1 * SWEEP_BX + threadIdx.x] : 0u;
+    channel2_cells<Q, ST, true>(a, x0, y, z, true, has1, l0, l1);
+  }
 }
 
-// Channel sweep.  BOUNDARY = false: every warp tile that is not listed (rows
-// away from the y/z faces, no solid within one step), launched over the whole
-// box, plain pulls.  BOUNDARY = true: the listed tiles (face rows and tiles next
-// to solids), resolved pulls, solid mask, and the body force: per-cell sums in
-// the arithmetic type, accumulated over cells in FP64 -- warp shuffles, per
-// block, then over blocks by the last block in block order -- into the
-// force-history slot of this step.
-template <int Q, class ST, class A, bool BOUNDARY, int MINB>
+// Channel sweep, one cell per thread, one warp tile per warp, over the whole
+// box: unlisted tiles pull plainly, listed tiles through the face-state tables
+// and their link words (solid cells zeroed).  The tile's listed position is
+// warp-uniform, so is the branch.
+template <int Q, class ST, class A, int MINB>
 __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kernel(const SweepArgs a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
   const int nx = a.L.nx, ny = a.L.ny;
-  const int lane = threadIdx.x, wid = threadIdx.y;
-  // One cell: pull, moments, (boundary: solid mask and force), relax, store.
-  auto cell_step = [&](int x, int y, int z, long long t, A &Fx, A &Fy, A &Fz) {
-    const bool valid = x < nx;
-    if (!valid) x = nx - 1;
-    const long long S = a.L.S;
-    const long long c = a.L.idx(x, y, z);
-    const E *__restrict__ fa = static_cast<const E *>(a.fa);
-    E *__restrict__ fb = static_cast<E *>(a.fb);
-    A f[Q];
-    bool solid_here = false;
-    if constexpr (BOUNDARY) {
-      const unsigned links = a.links_bits[t * SWEEP_BX + lane];
-      solid_here = mask_solid(a.mask, a.nxw, ny, x, y, z);
-      static_for(
-          [&](auto ic) {
-            constexpr int I = decltype(ic)::value;
-            f[I] = pull_resolved<Q, ST, A, I>(fa, c, S, x, y, z, links, a);
-          },
-          std::make_integer_sequence<int, Q>{});
-      if (valid && !solid_here) cell_force<Q, A, SF>(f, links, Fx, Fy, Fz);
-    } else {
-      static_for(
-          [&](auto ic) {
-            constexpr int I = decltype(ic)::value;
-            f[I] = pull_plain<Q, ST, A, I>(fa, c, S, x, a);
-          },
-          std::make_integer_sequence<int, Q>{});
-    }
-    A rho3, ux, uy, uz;
-    moments<L, A, SF>(f, rho3, ux, uy, uz);
-    if (solid_here) {
-      rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
-    }
-    const long long cell = ((long long)z * ny + y) * nx + x;
-    finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
-  };
-  // Boundary launch: a small persistent grid (about one block per SM, so it
-  // leaves most of every SM to the interior launch running beside it) strides
-  // over the listed tiles; each thread carries its force sums in FP64.
-  double dx = 0.0, dy = 0.0, dz = 0.0;
-  if constexpr (BOUNDARY) {
-    for (long long base = (long long)blockIdx.x * SWEEP_BY; base < a.n_slow;
-         base += (long long)gridDim.x * SWEEP_BY) {
-      const long long t = base + wid;
-      if (t >= a.n_slow) continue;  // warp-uniform
-      const int tile = a.slow_tiles[t];
-      const int row = tile / a.nxw;
-      A Fx = A(0), Fy = A(0), Fz = A(0);
-      cell_step((tile % a.nxw) * SWEEP_BX + lane, row % ny, row / ny, t, Fx, Fy, Fz);
-      if constexpr (sizeof(A) == 4) {
-        dx += f2d_bits(Fx);
-        dy += f2d_bits(Fy);
-        dz += f2d_bits(Fz);
-      } else {
-        dx += Fx;
-        dy += Fy;
-        dz += Fz;
-      }
-    }
+  const int lane = threadIdx.x;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y, z = blockIdx.z;
+  if (y >= ny) return;
+  const int t = a.tile_index[((long long)z * ny + y) * a.nxw + blockIdx.x];
+  int x = blockIdx.x * SWEEP_BX + lane;
+  const bool valid = x < nx;
+  if (!valid) x = nx - 1;
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  E *__restrict__ fb = static_cast<E *>(a.fb);
+  A f[Q];
+  bool solid_here = false;
+  if (t >= 0) {
+    const unsigned links = a.links_bits[(long long)t * SWEEP_BX + lane];
+    solid_here = links >> 31;
+    const int st = face_state(y, z, ny, a.L.nz);
+    const long long *__restrict__ offs = a.face_off + st * Q;
+    const unsigned wbb = a.face_bb[st];
+    static_for(
+        [&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          f[I] = pull_listed<Q, ST, A, I>(fa, c, S, x, offs[I], (wbb >> I) & 1u, links, a);
+        },
+        std::make_integer_sequence<int, Q>{});
   } else {
-    const int y = blockIdx.y * SWEEP_BY + wid;
-    const int z = blockIdx.z;
-    if (y >= ny || a.tile_slow[((long long)z * ny + y) * a.nxw + blockIdx.x]) return;  // whole warp
-    A Fx = A(0), Fy = A(0), Fz = A(0);
-    cell_step(blockIdx.x * SWEEP_BX + lane, y, z, 0, Fx, Fy, Fz);
+    static_for(
+        [&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          f[I] = pull_plain<Q, ST, A, I>(fa, c, S, x, a);
+        },
+        std::make_integer_sequence<int, Q>{});
   }
-  if constexpr (BOUNDARY) {
-    // Per-thread FP64 sums; block partial -> partials[blockIdx.x]; the last
-    // block sums all partials in block order.
-    constexpr int NW = SWEEP_BY;
-    const int tid = wid * SWEEP_BX + lane;
-    __shared__ double sh[3][NW];
-    __shared__ bool last;
-    for (int o = 16; o > 0; o >>= 1) {
-      dx += __shfl_down_sync(0xffffffffu, dx, o);
-      dy += __shfl_down_sync(0xffffffffu, dy, o);
-      dz += __shfl_down_sync(0xffffffffu, dz, o);
+  A rho3, ux, uy, uz;
+  moments<L, A, SF>(f, rho3, ux, uy, uz);
+  if (solid_here) {
+    rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
+  }
+  const long long cell = ((long long)z * ny + y) * nx + x;
+  finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
+}
+
+// Sums per-thread FP64 force partials of a persistent grid: warp shuffles, per
+// block into partials[blockIdx.x], then over blocks, in block order, by the last
+// block to finish, into the force-history slot of this step.
+__device__ __forceinline__ void force_to_history(const SweepArgs &a, double dx, double dy,
+                                                 double dz) {
+  constexpr int NW = SWEEP_BY;
+  const int lane = threadIdx.x, wid = threadIdx.y;
+  const int tid = wid * SWEEP_BX + lane;
+  __shared__ double sh[3][NW];
+  __shared__ bool last;
+  for (int o = 16; o > 0; o >>= 1) {
+    dx += __shfl_down_sync(0xffffffffu, dx, o);
+    dy += __shfl_down_sync(0xffffffffu, dy, o);
+    dz += __shfl_down_sync(0xffffffffu, dz, o);
+  }
+  if (lane == 0) {
+    sh[0][wid] = dx;
+    sh[1][wid] = dy;
+    sh[2][wid] = dz;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double bx = 0.0, by = 0.0, bz = 0.0;
+    for (int w = 0; w < NW; ++w) { bx += sh[0][w]; by += sh[1][w]; bz += sh[2][w]; }
+    a.partials[3 * blockIdx.x] = bx;
+    a.partials[3 * blockIdx.x + 1] = by;
+    a.partials[3 * blockIdx.x + 2] = bz;
+    __threadfence();
+    last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    const volatile double *p = a.partials;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (unsigned k = tid; k < gridDim.x; k += SWEEP_BX * SWEEP_BY) {
+      s0 += p[3 * k];
+      s1 += p[3 * k + 1];
+      s2 += p[3 * k + 2];
     }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+      s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    }
+    __syncthreads();
     if (lane == 0) {
-      sh[0][wid] = dx;
-      sh[1][wid] = dy;
-      sh[2][wid] = dz;
+      sh[0][wid] = s0;
+      sh[1][wid] = s1;
+      sh[2][wid] = s2;
     }
     __syncthreads();
     if (tid == 0) {
-      double bx = 0.0, by = 0.0, bz = 0.0;
-      for (int w = 0; w < NW; ++w) { bx += sh[0][w]; by += sh[1][w]; bz += sh[2][w]; }
-      a.partials[3 * blockIdx.x] = bx;
-      a.partials[3 * blockIdx.x + 1] = by;
-      a.partials[3 * blockIdx.x + 2] = bz;
-      __threadfence();
-      last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-      __threadfence();
-      const volatile double *p = a.partials;
-      double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-      for (unsigned k = tid; k < gridDim.x; k += SWEEP_BX * SWEEP_BY) {
-        s0 += p[3 * k];
-        s1 += p[3 * k + 1];
-        s2 += p[3 * k + 2];
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        s0 += __shfl_down_sync(0xffffffffu, s0, o);
-        s1 += __shfl_down_sync(0xffffffffu, s1, o);
-        s2 += __shfl_down_sync(0xffffffffu, s2, o);
-      }
-      __syncthreads();
-      if (lane == 0) {
-        sh[0][wid] = s0;
-        sh[1][wid] = s1;
-        sh[2][wid] = s2;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        double tx = 0.0, ty = 0.0, tz = 0.0;
-        for (int w = 0; w < NW; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
-        const long long st = *a.step;
-        double *h = a.hist + 3 * (st % a.cap);
-        h[0] = tx;
-        h[1] = ty;
-        h[2] = tz;
-        *a.step = st + 1;
-        *a.counter = 0u;
-      }
+      double tx = 0.0, ty = 0.0, tz = 0.0;
+      for (int w = 0; w < NW; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
+      const long long st = *a.step;
+      double *h = a.hist + 3 * (st % a.cap);
+      h[0] = tx;
+      h[1] = ty;
+      h[2] = tz;
+      *a.step = st + 1;
+      *a.counter = 0u;
     }
   }
+}
+
+// Momentum-exchange force on the solids for this step: a small persistent grid
+// (about one block per SM) on a second stream beside the sweep strides over
+// the listed tiles and, for every fluid cell with solid links, reads the
+// populations the sweep bounces back (f*_{opp(I)}(X) from the state it pulls
+// from); per cell the sum runs in the arithmetic type, over cells in FP64.
+template <int Q, class ST, class A, int MINB>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) channel_force_kernel(const SweepArgs a) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx, ny = a.L.ny;
+  const int lane = threadIdx.x, wid = threadIdx.y;
+  const long long S = a.L.S;
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  double dx = 0.0, dy = 0.0, dz = 0.0;
+  for (long long base = (long long)blockIdx.x * SWEEP_BY; base < a.n_slow;
+       base += (long long)gridDim.x * SWEEP_BY) {
+    const long long t = base + wid;
+    if (t >= a.n_slow) continue;  // warp-uniform
+    const unsigned word = a.links_bits[t * SWEEP_BX + lane];
+    const unsigned links = word & ~(1u << 31);
+    A Fx = A(0), Fy = A(0), Fz = A(0);
+    if (links && !(word >> 31)) {  // a fluid cell with solid links (x < nx: bits are 0 past nx)
+      const int tile = a.slow_tiles[t];
+      const int row = tile / a.nxw;
+      const long long c = a.L.idx((tile % a.nxw) * SWEEP_BX + lane, row % ny, row / ny);
+      A f[Q];
+      static_for(
+          [&](auto ic) {
+            constexpr int I = decltype(ic)::value;
+            f[I] = ((links >> I) & 1u)
+                       ? SF::template load<A, L>(fa + (long long)DirC<Q, I>::opp * S + c, I)
+                       : A(0);
+          },
+          std::make_integer_sequence<int, Q>{});
+      cell_force<Q, A, SF>(f, links, Fx, Fy, Fz);
+    }
+    if constexpr (sizeof(A) == 4) {
+      dx += f2d_bits(Fx);
+      dy += f2d_bits(Fy);
+      dz += f2d_bits(Fz);
+    } else {
+      dx += Fx;
+      dy += Fy;
+      dz += Fz;
+    }
+  }
+  (void)nx;
+  force_to_history(a, dx, dy, dz);
 }
 
 // Macroscopic fields of the step that read a.fa, formed on request instead of
@@ -654,7 +773,7 @@ void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) 
     }
     if (!wide) sweep_channel2_kernel<Q, ST, M2><<<g2, block, 0, s>>>(a);
   } else {
-    sweep_channel_kernel<Q, ST, A, false, MINB_FAST><<<grid, block, 0, s>>>(a);
+    sweep_channel_kernel<Q, ST, A, MINB_FAST><<<grid, block, 0, s>>>(a);
   }
 }
 
@@ -664,12 +783,12 @@ cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const Swe
   dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
   const int sb = a.bnd_blocks;
   if (fk && fk->side) {
-    // The listed tiles go first on the (higher-priority) side stream, so their
-    // latency-bound blocks overlap the interior kernel's streaming.
+    // The force launch goes first on the (higher-priority) side stream, so its
+    // latency-bound blocks overlap the sweep's streaming.
     cudaError_t e = cudaEventRecord(fk->fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(fk->side, fk->fork, 0);
     if (e != cudaSuccess) return e;
-    sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, fk->side>>>(a);
+    channel_force_kernel<Q, ST, A, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, fk->side>>>(a);
     e = cudaEventRecord(fk->join, fk->side);
     if (e != cudaSuccess) return e;
     launch_interior<Q, ST, A, MINB_FAST>(a, grid, block, s);
@@ -677,7 +796,7 @@ cudaError_t launch_sweep_channel_t(const SweepArgs &a, cudaStream_t s, const Swe
     if (e != cudaSuccess) return e;
   } else {
     launch_interior<Q, ST, A, MINB_FAST>(a, grid, block, s);
-    sweep_channel_kernel<Q, ST, A, true, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
+    channel_force_kernel<Q, ST, A, MINB_SLOW><<<sb > 0 ? sb : 1, block, 0, s>>>(a);
   }
   count_launch(2);
   return cudaGetLastError();
