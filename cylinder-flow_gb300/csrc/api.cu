@@ -228,10 +228,11 @@ void face_tables(const Layout &Ly, int wall_y, int wall_z, std::vector<long long
     }
 }
 
-// Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) holding a
-// solid cell or a cell with solid links: the second channel launch handles
-// them.  Fills the list and the 32 link words of every listed tile; returns the
-// per-tile flags.
+// Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) on a y/z face
+// row or holding a solid cell or a cell with solid links: the sweep pulls them
+// through the face-state tables and their link words, and the force launch
+// walks their list.  Fills the list and the 32 link words of every listed tile
+// (bit 31: solid cell); returns the per-tile flags.
 std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
                                        const std::vector<uint32_t> &bits, int nx, int ny,
                                        int nz, int nxw, std::vector<int> &list,
@@ -374,8 +375,8 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaEventCreateWithFlags(&h->ev_sync, cudaEventDisableTiming));
   CK_CUDA(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, cfg->device));
   if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
-    // Side stream of the channel sweep's listed-tile kernel, at the highest
-    // priority so its blocks are scheduled ahead of the interior kernel's.
+    // Side stream of the channel step's force kernel, at the highest priority
+    // so its blocks are scheduled ahead of the sweep's.
     int lo = 0, hi = 0;
     CK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     CK_CUDA(cudaStreamCreateWithPriority(&h->fork.side, cudaStreamNonBlocking, hi));

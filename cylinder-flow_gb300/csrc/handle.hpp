@@ -22,7 +22,7 @@ struct cflbm_handle {
   size_t f_bytes = 0;
   uint32_t *d_mask = nullptr;
   unsigned *d_links_bits = nullptr;  // link bits of the tiles next to solids
-  unsigned char *d_tile_slow = nullptr;  // per warp tile: needs the resolving kernel
+  unsigned char *d_tile_slow = nullptr;  // per warp tile: listed (face row or next to a solid)
   int *d_slow_tiles = nullptr;           // list of those tiles
   int *d_tile_index = nullptr;           // per warp tile: position in that list or -1
   long long *d_face_off = nullptr;       // listed-tile pull offsets per face state

@@ -74,12 +74,12 @@ struct SweepArgs {
                                // bit 31 = the cell is solid
   const long long *face_off;   // [16][Q] listed-tile pull offsets per face state
   const unsigned *face_bb;     // [16] directions bouncing back at a no-slip face
-  double *partials;      // 3 doubles per block of the resolving kernel
+  double *partials;      // 3 doubles per block of the force kernel
   unsigned int *counter; // finished force blocks (self-resetting)
   double *hist;          // force history, 3 doubles per step
   long long *step;       // device step counter (history slot = step % cap)
   long long cap;
-  int bnd_blocks;        // grid of the listed-tile launch (persistent, about one block per SM)
+  int bnd_blocks;        // grid of the force launch (persistent, about one block per SM)
 };
 
 struct FillArgs {
@@ -122,9 +122,9 @@ struct ReduceArgs {
 
 // ---- launchers (defined in the .cu files, dispatch on lattice and storage) ----
 cudaError_t launch_sweep(int Q, int store, int compute, const SweepArgs &a, cudaStream_t s);
-// Fork/join of the two channel-sweep launches: the listed-tile kernel runs on
-// `side` while the interior kernel runs on the main stream (they write disjoint
-// cells and only read the current state), joined before anything that follows.
+// Fork/join of the two launches of a channel step: the force kernel runs on
+// `side` while the sweep runs on the main stream (the force kernel only reads
+// the state the sweep reads), joined before anything that follows.
 struct SweepFork {
   cudaStream_t side;
   cudaEvent_t fork, join;
