@@ -146,7 +146,8 @@ def test_channel_fp64_matches_oracle(cuda, name):
                                                  ("fp32", "fp64", 2e-5),
                                                  ("fp16dev", "fp32", 3e-3)])
 def test_channel_reduced_precision_close_to_oracle(cuda, storage, compute, tol):
-    for name in ("d2q9_cyl_freeslip", "d3q27_cyl"):
+    # every wall combination: listed tiles pull through the face-state tables
+    for name in sorted(CHANNEL_CASES):
         case = CHANNEL_CASES[name]
         steps = 200 if case["lattice"] == 9 else 30
         o = oracle_channel(case, steps)
@@ -154,6 +155,20 @@ def test_channel_reduced_precision_close_to_oracle(cuda, storage, compute, tol):
         assert rel_err(r["u"], o["u"]) < tol, (name, storage, compute)
         assert rel_err(r["v"], o["v"]) < 20 * tol, (name, storage, compute)
         assert rel_err(r["force"][:, 0], o["force"][:, 0]) < 10 * tol, (name, storage, compute)
+
+
+@pytest.mark.parametrize("name", sorted(CHANNEL_CASES))
+def test_one_cell_and_pair_kernels_agree_bit_for_bit(cuda, name):
+    """FP32 collision on FP64 storage (one cell per thread) and on FP32 storage
+    (two cells per thread, packed FP32x2) hold the same FP32 values every step,
+    listed tiles included, so states and forces must be identical."""
+    case = CHANNEL_CASES[name]
+    steps = 60 if case["lattice"] == 9 else 12
+    a = gpu_channel(case, steps, storage="fp64", compute="fp32")
+    b = gpu_channel(case, steps, storage="fp32", compute="fp32")
+    assert np.array_equal(a["fpost"], b["fpost"]), name
+    assert np.array_equal(a["force"], b["force"]), name
+    assert np.array_equal(a["u"], b["u"]), name
 
 
 @pytest.mark.parametrize("storage,tol", [("fp32", 2e-5), ("fp16dev", 3e-3)])
