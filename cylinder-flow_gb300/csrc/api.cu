@@ -549,6 +549,9 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     cudaMemcpyAsync(dw, ref.w.data(), P * 8, cudaMemcpyHostToDevice, h->stream);
     cudaMemcpyAsync(dp, ref.p.data(), P * 8, cudaMemcpyHostToDevice, h->stream);
     cudaError_t e = launch_init_macros(Q, cfg->storage, L, h->fA, du, dv, dw, dp, h->stream);
+    // Both buffers start with the same ghost layers; afterwards only the face
+    // passes write ghosts, into both buffers.
+    if (e == cudaSuccess) e = launch_ghost_copy(Q, cfg->storage, L, h->fA, h->fB, h->stream);
     // Step-0 macroscopic fields: the interior of the initial fields.
     std::vector<double> mu(N), mv(N), mw(N), mp(N);
     const int lxp = nx + 2 * G, lyp = ny + 2 * G;
@@ -658,6 +661,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   FillArgs fa{};
   fa.L = L;
   fa.f = h->fA;
+  fa.f2 = h->fB;  // face-pass ghosts go to both buffers (see face_op_kernel)
   fa.mask = h->d_mask;
   fa.nxw = h->nxw;
   fa.wall_y = h->cfg.wall_y;
@@ -681,12 +685,16 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   }
   if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
     // "MPI Kokkos/lbm.cpp:315-345": inlet, outlet, then the two wall rows.
+    // Each pair (the two ends of one axis) writes and reads disjoint layers, so a
+    // pair runs as one launch; the pairs keep the reference's order.
     const FaceOp ops[4] = {{0, 0, 0}, {1, 0, 1}, {2, 1, 0}, {2, 1, 1}};
-    for (const FaceOp &op : ops) CK_CUDA(launch_face_op(Q, st, fa, op, h->stream));
+    for (int k = 0; k < 4; k += 2)
+      CK_CUDA(launch_face_ops(Q, st, fa, ops[k], ops[k + 1], h->stream));
   } else {
     // "3D MPI+KOKKOS+MPIIO/lbm.cpp:278-347": front, back, bottom, top, inlet, outlet.
     const FaceOp ops[6] = {{2, 1, 0}, {2, 1, 1}, {2, 2, 0}, {2, 2, 1}, {0, 0, 0}, {1, 0, 1}};
-    for (const FaceOp &op : ops) CK_CUDA(launch_face_op(Q, st, fa, op, h->stream));
+    for (int k = 0; k < 6; k += 2)
+      CK_CUDA(launch_face_ops(Q, st, fa, ops[k], ops[k + 1], h->stream));
   }
   LinkArgs la{};
   la.L = L;
@@ -727,7 +735,6 @@ static int one_step(cflbm_handle *h, bool write_macros) {
     if ((trc = record_event(h, &ts1))) return trc;
     h->sweep_ev.push_back({ts0, ts1});
   }
-  if (ref) CK_CUDA(launch_ghost_copy(Q, st, L, h->fA, h->fB, h->stream));
   std::swap(h->fA, h->fB);
   ++h->steps_done;
   return CFLBM_OK;

@@ -14,15 +14,11 @@ long long g_launches = 0;
 
 // Runtime direction tables (boundary kernels index directions dynamically).
 template <int Q> struct DT;
+__constant__ signed char c_e9[9][2] = {{0, 0}, {1, 0},  {0, 1},   {-1, 0}, {0, -1},
+                                        {1, 1}, {-1, 1}, {-1, -1}, {1, -1}};
 template <> struct DT<9> {
-  __device__ static int ex(int i) {
-    const int v[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
-    return v[i];
-  }
-  __device__ static int ey(int i) {
-    const int v[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
-    return v[i];
-  }
+  __device__ static int ex(int i) { return c_e9[i][0]; }
+  __device__ static int ey(int i) { return c_e9[i][1]; }
   __device__ static int ez(int) { return 0; }
 };
 __constant__ signed char c_e27[27][3] = {
@@ -36,6 +32,11 @@ template <> struct DT<27> {
   __device__ static int ez(int i) { return c_e27[i][2]; }
 };
 template <int Q> __device__ int dopp(int i) { return Lat<Q>::opp(i); }
+// D2Q9 opposite for a run-time index, without a table in local memory:
+// 1<->3, 2<->4 (axes), 5<->7, 6<->8 (diagonals).
+template <> __device__ int dopp<9>(int i) {
+  return i == 0 ? 0 : (i <= 4 ? (i + 1) % 4 + 1 : (i - 3) % 4 + 5);
+}
 template <int Q> __device__ int dmirror(int i, int d) {
   int w0 = DT<Q>::ex(i), w1 = DT<Q>::ey(i), w2 = DT<Q>::ez(i);
   if (d == 1) w1 = -w1;
@@ -154,58 +155,70 @@ __global__ void fill_channel_kernel(const FillArgs a) {
 //          (:278-324, :331-345).
 // Tangential ranges cover the interior plus one ring, [-1, n+1), as the
 // reference's [ghost-1, l-ghost+1).
+// No cell a pass writes is read by the same pass (it writes layer -1 or n of its
+// axis and reads layer 0, nx-1 or two layers in), so every (population, face
+// cell) is an independent thread.  The values also go to the other buffer
+// (a.f2): the ghost layers then carry the same values in both buffers, as in the
+// reference's single array, and the sweep, which writes only the interior, needs
+// no ghost copy.
 template <int Q, class ST>
-__global__ void face_op_kernel(const FillArgs a, const FaceOp op) {
+__global__ void face_op_kernel(const FillArgs a, const FaceOp op0, const FaceOp op1) {
+  // Two passes of one axis in one launch (grid z: population of op0, then of
+  // op1): the two faces of an axis write different layers and read neither's.
+  const bool second = (int)blockIdx.z >= op0.ndir;
+  const int kdir = (int)blockIdx.z - (second ? op0.ndir : 0);
+  const int kind = second ? op1.kind : op0.kind, side = second ? op1.side : op0.side;
   using E = typename Store<ST>::elem;
   E *f = static_cast<E *>(a.f);
+  E *f2 = static_cast<E *>(a.f2);
   const Layout &L = a.L;
   const bool d3 = (Q == 27);
-  const int n[3] = {L.nx, L.ny, L.nz};
-  const int ta = (op.axis == 0) ? 1 : 0;
-  const int tb = (op.axis == 2) ? 1 : 2;
-  const int na = n[ta] + 2;
-  const int nb = d3 ? n[tb] + 2 : 1;
+  const int ax = op0.axis;
+  const int nax = ax == 0 ? L.nx : (ax == 1 ? L.ny : L.nz);
+  const int na = (ax == 0 ? L.ny : L.nx) + 2;               // first tangential axis
+  const int nb = d3 ? (ax == 2 ? L.ny : L.nz) + 2 : 1;      // second tangential axis
   const int b0 = d3 ? -1 : 0;
-  const long long total = (long long)na * nb;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int pa = (int)(t % na) - 1;
-    const int pb = (int)(t / na) + b0;
-    for (int i = 0; i < Q; ++i) {
-      const int e[3] = {DT<Q>::ex(i), DT<Q>::ey(i), DT<Q>::ez(i)};
-      const int ea = e[op.axis];
-      int dst[3], src[3];
-      int srcpop = i;
-      dst[ta] = pa;
-      dst[tb] = pb;
-      if (op.kind == 0) {
-        if (ea <= 0) continue;
-        dst[op.axis] = -1;
-        src[0] = 0; src[ta] = pa; src[tb] = pb;
-      } else if (op.kind == 1) {
-        if (ea >= 0) continue;
-        dst[op.axis] = n[op.axis];
-        src[0] = n[0] - 1;
-        src[ta] = pa + e[ta];
-        src[tb] = pb + e[tb];
-      } else {
-        if (op.side == 0 ? (ea <= 0) : (ea >= 0)) continue;
-        dst[op.axis] = op.side == 0 ? -1 : n[op.axis];
-        src[op.axis] = op.side == 0 ? 1 : n[op.axis] - 2;
-        src[ta] = pa + 2 * e[ta];
-        src[tb] = pb + 2 * e[tb];
-        srcpop = dopp<Q>(i);
-      }
-      if (!d3) { dst[2] = 0; src[2] = 0; }
-      f[i * L.S + L.idx(dst[0], dst[1], dst[2])] =
-          f[srcpop * L.S + L.idx(src[0], src[1], src[2])];
-    }
+  (void)nb;
+  // (axis value, tangential a, tangential b) -> (x, y, z)
+  auto cell = [&](int v, int ta, int tb) -> long long {
+    const int x = ax == 0 ? v : ta;
+    const int y = ax == 1 ? v : (ax == 0 ? ta : tb);
+    const int z = d3 ? (ax == 2 ? v : tb) : 0;
+    return L.idx(x, y, z);
+  };
+  // One thread per (population, face cell): grid x along the first tangential
+  // axis, y the second, z the populations the pass writes (no index division).
+  const int i = (int)(((second ? op1.dirs : op0.dirs) >> (5 * kdir)) & 31u);
+  const int pa = blockIdx.x * blockDim.x + threadIdx.x - 1;
+  const int pb = blockIdx.y + b0;
+  if (pa >= na - 1) return;
+  const int ex = DT<Q>::ex(i), ey = DT<Q>::ey(i), ez = DT<Q>::ez(i);
+  const int ea = ax == 0 ? ex : (ax == 1 ? ey : ez);
+  const int eta = ax == 0 ? ey : ex;                        // e along tangential a
+  const int etb = ax == 2 ? ey : ez;                        // e along tangential b
+  long long dst, src;
+  int srcpop = i;
+  if (kind == 0) {             // inlet copy (x axis)
+    if (ea <= 0) return;
+    dst = cell(-1, pa, pb);
+    src = cell(0, pa, pb);
+  } else if (kind == 1) {      // outlet extrapolation (x axis)
+    if (ea >= 0) return;
+    dst = cell(nax, pa, pb);
+    src = cell(L.nx - 1, pa + eta, pb + etb);
+  } else {                     // wall bounce
+    if (side == 0 ? (ea <= 0) : (ea >= 0)) return;
+    dst = cell(side == 0 ? -1 : nax, pa, pb);
+    src = cell(side == 0 ? 1 : nax - 2, pa + 2 * eta, pb + 2 * etb);
+    srcpop = dopp<Q>(i);
   }
+  const E v = f[srcpop * L.S + src];
+  f[i * L.S + dst] = v;
+  if (f2) f2[i * L.S + dst] = v;
 }
 
-// Keep the ghost layers of the single-array reference semantics: after the sweep
-// wrote B's interior, B's ghosts take A's (so values a pass does not rewrite
-// persist from step to step, as in the reference's one f array).
+// Ghost layers of A copied into B: once, after the initial fields are written,
+// so that both buffers start with the reference's initial ghost values.
 template <int Q, class ST>
 __global__ void ghost_copy_kernel(const Layout L, const void *src_, void *dst_) {
   using E = typename Store<ST>::elem;
@@ -506,12 +519,32 @@ cudaError_t launch_fill_channel(int Q, int store, const FillArgs &a, cudaStream_
   return cudaGetLastError();
 }
 
-cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaStream_t s) {
+// The populations a pass writes: e along its axis positive (inlet copy, low wall)
+// or negative (outlet extrapolation, high wall) -- 9 in D3Q27, 3 in D2Q9.
+static void face_dirs(int Q, FaceOp &op) {
+  op.ndir = 0;
+  op.dirs = 0;
+  for (int i = 1; i < Q; ++i) {
+    const int e[3] = {Q == 27 ? Lat<27>::ex(i) : Lat<9>::ex(i),
+                      Q == 27 ? Lat<27>::ey(i) : Lat<9>::ey(i),
+                      Q == 27 ? Lat<27>::ez(i) : 0};
+    const int ea = e[op.axis];
+    const bool want = op.kind == 0 ? ea > 0 : (op.kind == 1 ? ea < 0 : (op.side == 0 ? ea > 0 : ea < 0));
+    if (want && op.ndir < 9) op.dirs |= (unsigned long long)i << (5 * op.ndir++);
+  }
+}
+
+cudaError_t launch_face_ops(int Q, int store, const FillArgs &a, FaceOp op0, FaceOp op1,
+                            cudaStream_t s) {
+  if (op0.axis != op1.axis) return cudaErrorInvalidValue;
+  face_dirs(Q, op0);
+  face_dirs(Q, op1);
+  if (op0.ndir != op1.ndir || op0.ndir == 0) return cudaErrorInvalidValue;
   const int n[3] = {a.L.nx, a.L.ny, a.L.nz};
-  const int ta = (op.axis == 0) ? 1 : 0, tb = (op.axis == 2) ? 1 : 2;
-  const long long total = (long long)(n[ta] + 2) * (Q == 27 ? n[tb] + 2 : 1);
-  const int blocks = blocks_for(total, 128);
-  CFLBM_DISPATCH(Q, store, (face_op_kernel<QQ, ST><<<blocks, 128, 0, s>>>(a, op)));
+  const int ta = (op0.axis == 0) ? 1 : 0, tb = (op0.axis == 2) ? 1 : 2;
+  const dim3 grid((unsigned)((n[ta] + 2 + 127) / 128), (unsigned)(Q == 27 ? n[tb] + 2 : 1),
+                  (unsigned)(2 * op0.ndir));
+  CFLBM_DISPATCH(Q, store, (face_op_kernel<QQ, ST><<<grid, 128, 0, s>>>(a, op0, op1)));
   count_launch();
   return cudaGetLastError();
 }

@@ -85,6 +85,7 @@ struct SweepArgs {
 struct FillArgs {
   Layout L;
   void *f;               // state being filled (in place)
+  void *f2;              // the other buffer: face passes write their ghosts here too (or null)
   const uint32_t *mask;
   int nxw;
   int wall_y, wall_z;
@@ -95,6 +96,8 @@ struct FaceOp {
   int kind;  // 0 copy (inlet), 1 extrapolate (outlet), 2 bounce (wall)
   int axis;  // 0 x, 1 y, 2 z
   int side;  // 0 low, 1 high
+  int ndir;  // the populations the pass writes (filled by launch_face_ops),
+  unsigned long long dirs;  // 5 bits each, the k-th at bit 5k
 };
 
 struct LinkArgs {
@@ -138,7 +141,9 @@ cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs 
 // (the solid-tile launch runs 4 listed warp tiles per block).
 constexpr int SWEEP_BX = 32, SWEEP_BY = 4;
 cudaError_t launch_fill_channel(int Q, int store, const FillArgs &a, cudaStream_t s);
-cudaError_t launch_face_op(int Q, int store, const FillArgs &a, FaceOp op, cudaStream_t s);
+// Two face passes of one axis (independent of each other) in one launch.
+cudaError_t launch_face_ops(int Q, int store, const FillArgs &a, FaceOp op0, FaceOp op1,
+                            cudaStream_t s);
 cudaError_t launch_ghost_copy(int Q, int store, const Layout &L, const void *src, void *dst,
                               cudaStream_t s);
 cudaError_t launch_links(int Q, int store, const LinkArgs &a, int blocks, cudaStream_t s);
