@@ -496,9 +496,16 @@ def run_reference(args):
 
 
 def run_profile(args):
-    """A bare stepping loop for profiler captures (no extras, no CPU baseline)."""
+    """A bare stepping loop for profiler captures (no extras, no CPU baseline).
+    --ref: the reference-rule D3Q27 profile (the reference's face passes, sphere
+    and solid rule) on the same grid instead of the channel problem."""
     import cflbm
-    wl = dict(WORKLOAD, nx=args.nx, ny=args.ny, nz=args.nz, cx=args.nx / 4.0, cy=args.ny / 2.0)
+    if args.ref:
+        wl = dict(lattice=27, nx=args.nx, ny=args.ny, nz=args.nz, profile="ref3d", tau0=TAU0,
+                  u0=U_IN)
+    else:
+        wl = dict(WORKLOAD, nx=args.nx, ny=args.ny, nz=args.nz, cx=args.nx / 4.0,
+                  cy=args.ny / 2.0)
     with cflbm.Solver(storage=args.storage, compute=args.compute, layout=args.layout,
                       **wl) as s:
         s.step(args.warmup)
@@ -509,7 +516,8 @@ def run_profile(args):
         dt = time.perf_counter() - t0
         info = s.info()
     cells = args.nx * args.ny * args.nz
-    print(json.dumps({"profile_case": [args.nx, args.ny, args.nz], "storage": args.storage,
+    print(json.dumps({"profile_case": [args.nx, args.ny, args.nz],
+                      "profile": "ref3d" if args.ref else "channel", "storage": args.storage,
                       "compute": args.compute, "steps": args.steps,
                       "mlups_wall": cells * args.steps / dt / 1e6,
                       "bytes_per_cell": info.bytes_per_cell_step,
@@ -533,6 +541,8 @@ def main():
     ap.add_argument("--cpu-steps-2d", type=int, default=4000)
     ap.add_argument("--profile", action="store_true",
                     help="bare stepping loop on an --nx/--ny/--nz grid for profiler captures")
+    ap.add_argument("--ref", action="store_true",
+                    help="with --profile: the reference-rule D3Q27 profile")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=NZ)
