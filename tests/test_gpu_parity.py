@@ -107,6 +107,12 @@ CHANNEL_CASES = {
     "d3q27_noslip": dict(lattice=27, nx=40, ny=18, nz=16, tau0=0.05, u0=0.03,
                          wall_y="noslip", wall_z="noslip", geom="sphere", cx=12, cy=9,
                          cz=8, diam=6),
+    # narrower than one 32-cell tile, at the smallest y / z extents (4 cells)
+    "d2q9_narrow": dict(lattice=9, nx=20, ny=5, nz=1, tau0=0.05, u0=0.04,
+                        wall_y="noslip", geom="cylinder", cx=6, cy=2, diam=2.5),
+    "d3q27_narrow": dict(lattice=27, nx=21, ny=4, nz=4, tau0=0.05, u0=0.03,
+                         wall_y="periodic", wall_z="freeslip", geom="sphere", cx=7, cy=2,
+                         cz=2, diam=2.5),
 }
 
 
