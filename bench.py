@@ -281,7 +281,7 @@ def run_gb300(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded perturbation; no dataset)",
         "config": {"workload": "D3Q27 512x128x128 spanwise cylinder D=32, Re=200, "
-                               "free-slip y, periodic z (BASELINE configs[1])",
+                               "free-slip y, periodic z",
                    "storage": "f64", "collision": "f32", "global_cells": CELLS * world,
                    "parallelism": f"replicas x{world}",
                    "l2": "working set 2 x 3.8 GB >> 129 MB L2 (no flush needed)"},
@@ -403,7 +403,7 @@ def run_channel2d(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded perturbation; no dataset)",
         "config": {"workload": "D2Q9 400x100 cylinder channel D=20, Re=100, free-slip walls, "
-                               "20,000 steps (BASELINE configs[0])",
+                               "20,000 steps",
                    "storage": "f64", "collision": "f64", "global_cells": CH2D_CELLS * world,
                    "parallelism": f"replicas x{world}",
                    "l2": "working set 2 x 2.9 MB, L2-resident (the problem's own size)"},

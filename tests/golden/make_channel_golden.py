@@ -1,6 +1,6 @@
 """Oracle fixtures for the benchmark channel problem (no reference counterpart).
 
-The reference hard-codes its own boundaries and geometry, so the BASELINE
+The reference hard-codes its own boundaries and geometry, so the benchmark
 channel problems are pinned to the CPU oracle (oracle/lbm_oracle.cpp, itself
 pinned bit-for-bit to the reference's sources on the shared physics).  This
 script runs the oracle on the small 2-D benchmark problem -- D2Q9 400x100,
