@@ -226,13 +226,14 @@ def run_gb300(args):
     extra = {}
     if not args.quick:
         for name, st, cp, lay in (("fp64_arith", "fp64", "fp64", "rows"),
+                                  ("df64_arith", "fp64", "df64", "rows"),
                                   ("fp64_store_soa", "fp64", "fp32", "soa"),
                                   ("fp32_store", "fp32", "fp32", "rows"),
                                   ("fp32_store_soa", "fp32", "fp32", "soa"),
                                   ("fp16dev_store", "fp16dev", "fp32", "rows"),
                                   ("fp16dev_store_soa", "fp16dev", "fp32", "soa")):
             v = variant_mlups(cflbm, local, st, cp, lay,
-                              max(steps // 5, 20) if cp == "fp64" else steps // 2,
+                              max(steps // 5, 20) if cp != "fp32" else steps // 2,
                               min(warmup, 5))
             v["hbm_frac"] = v["bytes_per_cell"] * CELLS / (v["sweep_us"] * 1e-6) / 1e9 / peak
             extra[name] = {k: round(x, 4) if isinstance(x, float) else x for k, x in v.items()}
@@ -547,7 +548,7 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=NZ)
     ap.add_argument("--storage", default="fp64", choices=["fp64", "fp32", "fp16dev"])
-    ap.add_argument("--compute", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--compute", default="fp32", choices=["fp64", "fp32", "df64"])
     ap.add_argument("--layout", default="rows", choices=["soa", "rows"])
     args = ap.parse_args()
     args.steps_ref = 1

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(_HERE, "libcflbm.so")
 
 D2Q9, D3Q27 = 9, 27
 STORE_FP64, STORE_FP32, STORE_FP16DEV = 0, 1, 2
-COMPUTE_FP64, COMPUTE_FP32 = 0, 1
+COMPUTE_FP64, COMPUTE_FP32, COMPUTE_DF64 = 0, 1, 2
 PROFILE_CHANNEL, PROFILE_REF2D, PROFILE_REF3D = 0, 1, 2
 WALL_FREESLIP, WALL_NOSLIP, WALL_PERIODIC = 0, 1, 2
 GEOM_NONE, GEOM_CYLINDER, GEOM_SPHERE = 0, 1, 2

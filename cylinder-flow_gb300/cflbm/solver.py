@@ -25,7 +25,7 @@ class Solver:
 
     _names = {
         "storage": {"fp64": C.STORE_FP64, "fp32": C.STORE_FP32, "fp16dev": C.STORE_FP16DEV},
-        "compute": {"fp64": C.COMPUTE_FP64, "fp32": C.COMPUTE_FP32},
+        "compute": {"fp64": C.COMPUTE_FP64, "fp32": C.COMPUTE_FP32, "df64": C.COMPUTE_DF64},
         "profile": {"channel": C.PROFILE_CHANNEL, "ref2d": C.PROFILE_REF2D,
                     "ref3d": C.PROFILE_REF3D},
         "wall_y": {"freeslip": C.WALL_FREESLIP, "noslip": C.WALL_NOSLIP,

@@ -307,8 +307,10 @@ int validate(const cflbm_config *c) {
     return fail(CFLBM_E_INVALID, "ny or nz exceeds the launch grid limit");
   if (c->storage < 0 || c->storage > 2)
     return fail(CFLBM_E_INVALID, "storage %d unknown", c->storage);
-  if (c->compute < 0 || c->compute > 1)
+  if (c->compute < 0 || c->compute > 2)
     return fail(CFLBM_E_INVALID, "compute %d unknown", c->compute);
+  if (c->compute == CFLBM_COMPUTE_DF64 && c->storage != CFLBM_STORE_FP64)
+    return fail(CFLBM_E_INVALID, "double-float arithmetic needs FP64 storage");
   if (c->profile < 0 || c->profile > 2)
     return fail(CFLBM_E_INVALID, "profile %d unknown", c->profile);
   if (c->profile == CFLBM_PROFILE_REF2D && c->lattice != CFLBM_D2Q9)

@@ -125,6 +125,29 @@ __device__ __forceinline__ float d2f_bits(double d) {
   return __uint_as_float(t | (hi & 0x80000000u));
 }
 
+// Double-float number: the unevaluated sum hi + lo of two binary32 values,
+// |lo| <= ulp(hi) / 2, about 48 significant bits.  On GB300 the FP32 units run
+// at ~70 times the FP64 units' rate, so a collision in this arithmetic is
+// faster than in FP64 at near-FP64 accuracy (relative error per operation
+// ~2^-46 instead of 2^-53).  From and to FP64 storage: hi = d rounded to FP32,
+// lo = the exact remainder d - hi rounded to FP32, and back hi + lo; the
+// roundings use the integer converters above, so each costs one FP64 add or
+// subtract.  Only the channel and reference sweeps use it (compute = DF64).
+struct df64 {
+  float hi, lo;
+  df64() = default;
+  __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ df64(float f) : hi(f), lo(0.0f) {}
+  __device__ __forceinline__ df64(int i) : hi((float)i), lo(0.0f) {}
+  __device__ __forceinline__ df64(double d) {
+    hi = d2f_bits(d);
+    lo = d2f_bits(__dsub_rn(d, f2d_bits(hi)));
+  }
+  __device__ __forceinline__ operator double() const {
+    return __dadd_rn(f2d_bits(hi), f2d_bits(lo));
+  }
+};
+
 // Storage codecs.  load/store move values in "storage units": the population
 // times scale<L>(i) (1 for FP64 and FP32; the FP16 format's power of two), so
 // the FP16 path converts without a multiply; the sweep helpers fold 1/scale and

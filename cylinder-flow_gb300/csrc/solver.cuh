@@ -22,7 +22,7 @@ namespace cflbm {
 enum Profile { PROFILE_CHANNEL = 0, PROFILE_REF2D = 1, PROFILE_REF3D = 2 };
 enum Wall { WALL_FREESLIP = 0, WALL_NOSLIP = 1, WALL_PERIODIC = 2 };
 enum StoreKind { STORE_F64 = 0, STORE_F32 = 1, STORE_F16 = 2 };
-enum ComputeKind { COMPUTE_F64 = 0, COMPUTE_F32 = 1 };
+enum ComputeKind { COMPUTE_F64 = 0, COMPUTE_F32 = 1, COMPUTE_DF64 = 2 };
 enum LayoutKind { LAYOUT_SOA = 0, LAYOUT_ROWS = 1 };
 
 struct Layout {

@@ -76,6 +76,50 @@ template <> struct VA<float2> {
   __device__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 };
 
+// Double-float arithmetic (df64, lattice.cuh), from published error-free
+// transformations: Knuth's TwoSum, Dekker's Fast2Sum and the FMA-based exact
+// product, combined as in Joldes, Muller and Popescu, "Tight and rigorous error
+// bounds for basic building blocks of double-word arithmetic" (ACM TOMS 44(2),
+// 2017): the accurate double-word sum (their Algorithm 6, relative error
+// <= 3u^2) and the double-word product with FMAs (Algorithm 12, <= 5u^2),
+// u = 2^-24.  fma(a, b, c) is the product followed by the sum.
+__device__ __forceinline__ void two_sum_(float a, float b, float &s, float &t) {
+  s = __fadd_rn(a, b);
+  const float ap = __fsub_rn(s, b), bp = __fsub_rn(s, ap);
+  t = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+__device__ __forceinline__ void fast_two_sum_(float a, float b, float &s, float &t) {
+  s = __fadd_rn(a, b);
+  t = __fsub_rn(b, __fsub_rn(s, a));
+}
+template <> struct VA<df64> {
+  using S = double;
+  __device__ static df64 splat(double s) {  // constants: folded at compile time
+    const float h = (float)s;
+    return df64(h, (float)(s - (double)h));
+  }
+  __device__ static df64 add(df64 x, df64 y) {
+    float sh, sl, th, tl, vh, vl, zh, zl;
+    two_sum_(x.hi, y.hi, sh, sl);
+    two_sum_(x.lo, y.lo, th, tl);
+    fast_two_sum_(sh, __fadd_rn(sl, th), vh, vl);
+    fast_two_sum_(vh, __fadd_rn(tl, vl), zh, zl);
+    return df64(zh, zl);
+  }
+  __device__ static df64 sub(df64 x, df64 y) { return add(x, df64(-y.hi, -y.lo)); }
+  __device__ static df64 mul(df64 x, df64 y) {
+    const float ch = __fmul_rn(x.hi, y.hi);
+    const float cl1 = __fmaf_rn(x.hi, y.hi, -ch);
+    const float tl0 = __fmul_rn(x.lo, y.lo);
+    const float tl1 = __fmaf_rn(x.hi, y.lo, tl0);
+    const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
+    float zh, zl;
+    fast_two_sum_(ch, __fadd_rn(cl1, cl2), zh, zl);
+    return df64(zh, zl);
+  }
+  __device__ static df64 fma(df64 a, df64 b, df64 c) { return add(mul(a, b), c); }
+};
+
 // acc + K v with K = NUM / DEN a power of two (1 and -1 without a product).
 template <class V, int NUM, int DEN>
 __device__ __forceinline__ V acc_(V acc, V v) {

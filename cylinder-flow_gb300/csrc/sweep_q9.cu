@@ -4,6 +4,8 @@
 namespace cflbm {
 
 cudaError_t launch_sweep_q9(int store, int compute, const SweepArgs &a, cudaStream_t s) {
+  if (compute == COMPUTE_DF64)
+    return store == STORE_F64 ? launch_sweep_t<9, double, df64, 4>(a, s) : cudaErrorInvalidValue;
   if (compute == COMPUTE_F64) {
     switch (store) {
       case STORE_F64: return launch_sweep_t<9, double, double, 4>(a, s);
@@ -22,6 +24,9 @@ cudaError_t launch_sweep_q9(int store, int compute, const SweepArgs &a, cudaStre
 
 cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a,
                                      cudaStream_t s, const SweepFork *fk) {
+  if (compute == COMPUTE_DF64)
+    return store == STORE_F64 ? launch_sweep_channel_t<9, double, df64, 4, 2>(a, s, fk)
+                              : cudaErrorInvalidValue;
   if (compute == COMPUTE_F64) {
     switch (store) {
       case STORE_F64: return launch_sweep_channel_t<9, double, double, 4, 2>(a, s, fk);
@@ -40,6 +45,9 @@ cudaError_t launch_sweep_channel_q9(int store, int compute, const SweepArgs &a,
 
 cudaError_t launch_macros_channel_q9(int store, int compute, const SweepArgs &a,
                                       cudaStream_t s) {
+  if (compute == COMPUTE_DF64)
+    return store == STORE_F64 ? launch_macros_channel_t<9, double, df64>(a, s)
+                              : cudaErrorInvalidValue;
   if (compute == COMPUTE_F64) {
     switch (store) {
       case STORE_F64: return launch_macros_channel_t<9, double, double>(a, s);

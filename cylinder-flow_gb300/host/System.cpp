@@ -48,7 +48,8 @@ void System::read(const std::string &path) {
         storage = v == "fp32" ? CFLBM_STORE_FP32 : v == "fp16dev" ? CFLBM_STORE_FP16DEV
                                                                    : CFLBM_STORE_FP64;
       else if (key == "compute")
-        compute = v == "fp32" ? CFLBM_COMPUTE_FP32 : CFLBM_COMPUTE_FP64;
+        compute = v == "fp32" ? CFLBM_COMPUTE_FP32 : v == "df64" ? CFLBM_COMPUTE_DF64
+                                                                 : CFLBM_COMPUTE_FP64;
       else if (key == "geom")
         geom = v == "cylinder" ? CFLBM_GEOM_CYLINDER : v == "sphere" ? CFLBM_GEOM_SPHERE
                                                                       : CFLBM_GEOM_NONE;

@@ -9,7 +9,7 @@
 // Extension (ignored by the reference, which stops after nine numbers): after
 // the "=============" separator, lines of the form "cflbm.<key> <value>" set
 // solver options: lattice (9|27), profile (ref2d|ref3d|channel), storage
-// (fp64|fp32|fp16dev), compute (fp64|fp32), steps (overrides the derived Time),
+// (fp64|fp32|fp16dev), compute (fp64|fp32|df64), steps (overrides the derived Time),
 // inter, geom (none|cylinder|sphere), center (cx cy cz), diam, wall_y, wall_z
 // (freeslip|noslip|periodic), perturb (amplitude), seed.
 #ifndef CFLBM_HOST_SYSTEM_HPP

@@ -39,8 +39,10 @@ enum cflbm_lattice { CFLBM_D2Q9 = 9, CFLBM_D3Q27 = 27 };
 /* Population storage.  FP16DEV stores f_i / t_i (f_i is already the deviation
  * from t_i*rho0, as in the reference) as IEEE binary16. */
 enum cflbm_storage { CFLBM_STORE_FP64 = 0, CFLBM_STORE_FP32 = 1, CFLBM_STORE_FP16DEV = 2 };
-/* Arithmetic of the collision. */
-enum cflbm_compute { CFLBM_COMPUTE_FP64 = 0, CFLBM_COMPUTE_FP32 = 1 };
+/* Arithmetic of the collision.  DF64: double-float (pairs of binary32, about 48
+ * significant bits) on the FP32 units, with FP64 storage only; for the channel
+ * and reference profiles (not the adjoint or the batch). */
+enum cflbm_compute { CFLBM_COMPUTE_FP64 = 0, CFLBM_COMPUTE_FP32 = 1, CFLBM_COMPUTE_DF64 = 2 };
 /* Boundary/initial-condition profile.
  *  CHANNEL: the benchmark channel (equilibrium inlet, zero-gradient outlet,
  *           free-slip/no-slip/periodic walls, halfway bounce-back on solids).

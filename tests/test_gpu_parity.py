@@ -148,6 +148,41 @@ def test_channel_fp64_matches_oracle(cuda, name):
     assert rel_err(r["force"], o["force"]) < 1e-9, name
 
 
+@pytest.mark.parametrize("name", sorted(CHANNEL_CASES))
+def test_channel_df64_matches_oracle(cuda, name):
+    """Double-float collision (pairs of FP32, about 48 bits) on FP64 storage stays
+    within 1e-9 of the FP64 oracle (FP32 collision: 2e-5)."""
+    case = CHANNEL_CASES[name]
+    steps = 300 if case["lattice"] == 9 else 40
+    o = oracle_channel(case, steps)
+    r = gpu_channel(case, steps, storage="fp64", compute="df64")
+    for k in ("u", "v", "w", "p", "fpost"):
+        if k == "w" and case["lattice"] == 9:
+            continue
+        assert rel_err(r[k], o[k]) < 1e-9, (name, k)
+    assert rel_err(r["force"], o["force"]) < 1e-8, name
+
+
+def test_reference_profiles_df64_close_to_fp64(cuda):
+    g = load_golden("ref2d_96x40")
+    m = g["meta"]
+    a = ref2d_gpu(m["nx"], m["ny"], m["tau0"], m["u0"], g["ran"], m["steps"])
+    b = ref2d_gpu(m["nx"], m["ny"], m["tau0"], m["u0"], g["ran"], m["steps"], compute="df64")
+    for k in ("u", "v", "p", "fpost", "force"):
+        assert rel_err(b[k], a[k]) < 1e-10, k
+    nx, ny, nz = 40, 14, 16
+    ran = np.random.default_rng(3).integers(0, 100, size=(nx + 6, ny + 6, nz + 6)).astype(np.int32)
+    a = ref3d_gpu(nx, ny, nz, 0.0192, 0.04, ran, 30)
+    b = ref3d_gpu(nx, ny, nz, 0.0192, 0.04, ran, 30, compute="df64")
+    for k in ("u", "v", "w", "p", "fpost"):
+        assert rel_err(b[k], a[k]) < 1e-10, k
+
+
+def test_df64_needs_fp64_storage(cuda):
+    with pytest.raises(cflbm.CflbmError):
+        Solver(storage="fp32", compute="df64", **CHANNEL_CASES["d2q9_cyl_freeslip"])
+
+
 @pytest.mark.parametrize("storage,compute,tol", [("fp64", "fp32", 2e-5), ("fp32", "fp32", 2e-5),
                                                  ("fp32", "fp64", 2e-5),
                                                  ("fp16dev", "fp32", 3e-3)])
