@@ -78,3 +78,11 @@ def test_extension_keys_set_solver_options(system_exe, tmp_path):
 def test_missing_input_is_reported(system_exe, tmp_path):
     a, _ = read(system_exe, tmp_path / "does_not_exist.in")
     assert a[0] == "0"
+
+
+def test_extension_key_selects_double_float_collision(system_exe, tmp_path):
+    p = tmp_path / "input.in"
+    p.write_text("1.0  8.0  100\n0.05  100  10\n64  32  32\n=============\nrho R Re\n"
+                 "cflbm.compute df64\n")
+    _, b = read(system_exe, p)
+    assert b[1:4] == ["2", "0", "2"]  # profile REF3D, FP64 storage, double-float collision
