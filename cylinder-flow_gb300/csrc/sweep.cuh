@@ -43,8 +43,8 @@ __device__ __forceinline__ void static_for(F &&f, std::integer_sequence<int, Is.
   (f(std::integral_constant<int, Is>{}), ...);
 }
 
-// Collision arithmetic over V = float, double or float2 (two cells per thread,
-// GB300's packed FFMA2/FADD2/FMUL2).  Every operation is explicitly rounded, so
+// Collision arithmetic over V = float, double, float2 (two cells per thread,
+// GB300's packed FFMA2/FADD2/FMUL2) or df64 (double-float, below).  Every operation is explicitly rounded, so
 // the compiler neither contracts nor reorders: a cell gets the same bits from
 // every kernel that collides it, scalar or packed.
 template <class V> struct VA;
