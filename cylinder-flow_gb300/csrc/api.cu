@@ -601,6 +601,35 @@ static int record_event(cflbm_handle *h, size_t *idx) {
 
 extern "C++" {
 namespace cflbm {
+void set_relax(SweepArgs &a, int Q, int store, double omega) {
+  a.omega = omega;
+  a.omega_f = (float)omega;
+  double rk[13] = {1.0 - omega};
+  for (int c = 0; c <= (Q == 27 ? 3 : 2); ++c) {
+    // weight and FP16 scale of class c (|e|^2 = c): the first direction of it
+    int i = 0;
+    for (int k = 0; k < Q; ++k) {
+      const int ex = Q == 27 ? Lat<27>::ex(k) : Lat<9>::ex(k);
+      const int ey = Q == 27 ? Lat<27>::ey(k) : Lat<9>::ey(k);
+      const int ez = Q == 27 ? Lat<27>::ez(k) : 0;
+      if (ex * ex + ey * ey + ez * ez == c) { i = k; break; }
+    }
+    const double w = Q == 27 ? Lat<27>::w(i) : Lat<9>::w(i);
+    const double sc = store != CFLBM_STORE_FP16DEV
+                          ? 1.0
+                          : (Q == 27 ? (double)Lat<27>::h_scale(i) : (double)Lat<9>::h_scale(i));
+    const double kw = omega * w * sc;
+    rk[1 + c] = kw;
+    rk[5 + c] = 4.5 * kw;
+    rk[9 + c] = 3.0 * kw;
+  }
+  for (int k = 0; k < 13; ++k) {
+    a.rk[k] = rk[k];
+    a.rkf[k] = (float)rk[k];
+    a.rkl[k] = (float)(rk[k] - (double)a.rkf[k]);
+  }
+}
+
 // Arguments of the channel sweep of handle h reading fa and writing fb.
 SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool write_macros) {
   SweepArgs sa{};
@@ -609,8 +638,7 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   sa.fb = fb;
   sa.mask = h->d_mask;
   sa.nxw = h->nxw;
-  sa.omega = h->omega;
-  sa.omega_f = (float)h->omega;
+  set_relax(sa, h->Q, h->cfg.storage, h->omega);
   sa.alpha = h->d_alpha;
   if (write_macros) {
     sa.mu = h->d_mu;
@@ -627,6 +655,7 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
                           : (h->Q == 27 ? (double)Lat<27>::h_scale(i) : (double)Lat<9>::h_scale(i));
     sa.f_in[i] = h->f_in[i] * sc;
     sa.f_in_f[i] = (float)(h->f_in[i] * sc);
+    sa.f_in_l[i] = (float)(h->f_in[i] * sc - (double)sa.f_in_f[i]);
   }
   // Persistent grid of the force launch beside the sweep: one block per SM
   // (measured on the D3Q27 512x128x128 bench step: 1 / 2 / 4 per SM give FP32
@@ -721,8 +750,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   sa.fb = h->fB;
   sa.mask = h->d_mask;
   sa.nxw = h->nxw;
-  sa.omega = h->omega;
-  sa.omega_f = (float)h->omega;
+  set_relax(sa, Q, st, h->omega);
   sa.ref_override = ref ? 1 : 0;
   sa.inlet_u = h->d_inlet;
   sa.alpha = h->d_alpha;

@@ -126,13 +126,16 @@ __device__ __forceinline__ float d2f_bits(double d) {
 }
 
 // Double-float number: the unevaluated sum hi + lo of two binary32 values,
-// |lo| <= ulp(hi) / 2, about 48 significant bits.  On GB300 the FP32 units run
-// at ~70 times the FP64 units' rate, so a collision in this arithmetic is
-// faster than in FP64 at near-FP64 accuracy (relative error per operation
-// ~2^-46 instead of 2^-53).  From and to FP64 storage: hi = d rounded to FP32,
-// lo = the exact remainder d - hi rounded to FP32, and back hi + lo; the
-// roundings use the integer converters above, so each costs one FP64 add or
-// subtract.  Only the channel and reference sweeps use it (compute = DF64).
+// about 47 significant bits.  On GB300 the FP32 units run at ~70 times the
+// FP64 units' rate, so a collision in this arithmetic is faster than in FP64
+// at near-FP64 accuracy.  From FP64 storage, with integer operations and one
+// FP32 subtraction (no FP64 unit): hi = d truncated to 24 significant bits,
+// lo = the next 23 bits of d, formed as the float with hi's sign, exponent
+// E - 23 and those bits as mantissa minus the same float with a zero mantissa
+// (an exact subtraction); |d - (hi + lo)| < 2^-46 |d|.  |d| < 2^-100 loads as
+// zero; |d| >= 2^128, infinities and NaNs load as NaN.  To FP64 storage:
+// hi + lo with the exact integer conversions above and one FP64 addition.
+// Only the channel and reference sweeps use it (compute = DF64).
 struct df64 {
   float hi, lo;
   df64() = default;
@@ -140,12 +143,28 @@ struct df64 {
   __device__ __forceinline__ df64(float f) : hi(f), lo(0.0f) {}
   __device__ __forceinline__ df64(int i) : hi((float)i), lo(0.0f) {}
   __device__ __forceinline__ df64(double d) {
-    hi = d2f_bits(d);
-    lo = d2f_bits(__dsub_rn(d, f2d_bits(hi)));
+    const unsigned hw = (unsigned)__double2hiint(d), lw = (unsigned)__double2loint(d);
+    const unsigned mag = hw & 0x7FFFFFFFu;
+    // exponent (rebased by 1023 - 127 = 896, mod 2^32) and the top 23 mantissa bits
+    const unsigned t = __funnelshift_l(lw, hw, 3) - 0xC0000000u;
+    const unsigned hb = (t & 0x7FFFFFFFu) | (hw & 0x80000000u);
+    const unsigned mg = (hb & 0xFF800000u) - (23u << 23);
+    const unsigned lb = mg | ((lw >> 6) & 0x7FFFFFu);
+    const bool tiny = mag < ((1023u - 100u) << 20);
+    const bool big = mag >= (1151u << 20);
+    hi = tiny ? 0.0f : (big ? __uint_as_float(0x7FC00000u) : __uint_as_float(hb));
+    lo = tiny ? 0.0f : __fsub_rn(__uint_as_float(lb), __uint_as_float(mg));
   }
   __device__ __forceinline__ operator double() const {
     return __dadd_rn(f2d_bits(hi), f2d_bits(lo));
   }
+};
+
+// Two cells' double-float numbers, component-wise (packed FP32x2 arithmetic).
+struct df64x2 {
+  float2 hi, lo;
+  df64x2() = default;
+  __device__ __forceinline__ df64x2(float2 h, float2 l) : hi(h), lo(l) {}
 };
 
 // Storage codecs.  load/store move values in "storage units": the population

@@ -58,6 +58,12 @@ struct SweepArgs {
   int nxw;               // mask words per row
   float omega_f;
   double omega;
+  // Relaxation constants (1 - omega and omega times the weight-class factors,
+  // storage scale included; layout in sweep.cuh, RK_*): FP64, FP32, and the
+  // FP32 remainder rk - rkf for double-float arithmetic.
+  double rk[13];
+  float rkf[13];
+  float rkl[13];
   int ref_override;      // reference profiles: inlet u at x = 0, p = 0 at x = nx-1
   const double *inlet_u; // ny*nz inlet velocity profile (reference profiles)
   const float *alpha;    // nx*ny*nz Brinkman porosity or null
@@ -66,6 +72,7 @@ struct SweepArgs {
   int wall_y, wall_z;
   double f_in[27];       // inlet equilibrium populations (p = 0, u = (u_in, 0, 0))
   float f_in_f[27];      // the same in FP32 (FP32-arithmetic sweeps)
+  float f_in_l[27];      // f_in - f_in_f in FP32 (double-float sweeps)
   const unsigned char *tile_slow;  // per warp tile (32 cells of a row): 1 = next to a solid
   const int *slow_tiles; // list of tiles next to solids (tile = (z*ny + y)*nxw + x/32)
   const int *tile_index; // per warp tile: its position in slow_tiles, -1 if not listed
@@ -161,6 +168,10 @@ cudaError_t launch_get_f(int Q, int store, const Layout &L, const void *f, doubl
 cudaError_t launch_set_f(int Q, int store, const Layout &L, void *f, const double *in,
                          cudaStream_t s);
 cudaError_t launch_fill_value(int Q, int store, const Layout &L, void *f, cudaStream_t s);
+
+// Fill omega, omega_f and the relaxation constants rk/rkf/rkl of a sweep for
+// lattice Q, storage kind `store` (the FP16 format's scales are folded in).
+void set_relax(SweepArgs &a, int Q, int store, double omega);
 
 // Number of kernel launches issued through the launchers (all handles).
 long long launches();

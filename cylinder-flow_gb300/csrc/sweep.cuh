@@ -76,48 +76,94 @@ template <> struct VA<float2> {
   __device__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 };
 
-// Double-float arithmetic (df64, lattice.cuh), from published error-free
-// transformations: Knuth's TwoSum, Dekker's Fast2Sum and the FMA-based exact
-// product, combined as in Joldes, Muller and Popescu, "Tight and rigorous error
-// bounds for basic building blocks of double-word arithmetic" (ACM TOMS 44(2),
-// 2017): the accurate double-word sum (their Algorithm 6, relative error
-// <= 3u^2) and the double-word product with FMAs (Algorithm 12, <= 5u^2),
-// u = 2^-24.  fma(a, b, c) is the product followed by the sum.
-__device__ __forceinline__ void two_sum_(float a, float b, float &s, float &t) {
-  s = __fadd_rn(a, b);
-  const float ap = __fsub_rn(s, b), bp = __fsub_rn(s, ap);
-  t = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+// Double-float arithmetic (df64 and its two-cell form df64x2, lattice.cuh)
+// from published error-free transformations: Knuth's TwoSum, Dekker's Fast2Sum
+// and the FMA-based exact product (Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18, 1971; Joldes, Muller and
+// Popescu, "Tight and rigorous error bounds for basic building blocks of
+// double-word arithmetic", ACM TOMS 44(2), 2017).
+//   add: Dekker's double-word sum (their Algorithm 5, "sloppy"): TwoSum of the
+//        high parts, the low parts added to its error, Fast2Sum -- 11
+//        operations; error <= 2u^2 (|x| + |y|) (u = 2^-24), relative to the
+//        operands, not the result, which is what a collision needs: every
+//        population is compared to the field, not to itself;
+//   mul: the exact product of the high parts plus the cross terms (the
+//        lo*lo term, ~u^2 of the product, dropped), Fast2Sum -- 8 operations;
+//        relative error <= 4u^2.
+// T = float (one cell) or float2 (two cells, GB300's packed FP32x2
+// instructions).
+template <class T> struct DWops {
+  using O = VA<T>;
+  __device__ static T neg(T a) { return O::sub(O::splat(0.0f), a); }
+  __device__ static void two_sum(T a, T b, T &s, T &t) {
+    s = O::add(a, b);
+    const T ap = O::sub(s, b), bp = O::sub(s, ap);
+    t = O::add(O::sub(a, ap), O::sub(b, bp));
+  }
+  __device__ static void fast_two_sum(T a, T b, T &s, T &t) {
+    s = O::add(a, b);
+    t = O::sub(b, O::sub(s, a));
+  }
+  __device__ static void add(T xh, T xl, T yh, T yl, T &zh, T &zl) {
+    T sh, e;
+    two_sum(xh, yh, sh, e);
+    e = O::add(e, O::add(xl, yl));
+    fast_two_sum(sh, e, zh, zl);
+  }
+  __device__ static void mul(T xh, T xl, T yh, T yl, T &zh, T &zl) {
+    const T ch = O::mul(xh, yh);
+    const T cl1 = O::fma(xh, yh, neg(ch));
+    const T cl2 = O::fma(xl, yh, O::mul(xh, yl));
+    fast_two_sum(ch, O::add(cl1, cl2), zh, zl);
+  }
+};
+template <> __device__ __forceinline__ float DWops<float>::neg(float a) { return -a; }
+template <> __device__ __forceinline__ float2 DWops<float2>::neg(float2 a) {
+  return make_float2(-a.x, -a.y);
 }
-__device__ __forceinline__ void fast_two_sum_(float a, float b, float &s, float &t) {
-  s = __fadd_rn(a, b);
-  t = __fsub_rn(b, __fsub_rn(s, a));
-}
+
 template <> struct VA<df64> {
   using S = double;
+  using D = DWops<float>;
   __device__ static df64 splat(double s) {  // constants: folded at compile time
     const float h = (float)s;
     return df64(h, (float)(s - (double)h));
   }
   __device__ static df64 add(df64 x, df64 y) {
-    float sh, sl, th, tl, vh, vl, zh, zl;
-    two_sum_(x.hi, y.hi, sh, sl);
-    two_sum_(x.lo, y.lo, th, tl);
-    fast_two_sum_(sh, __fadd_rn(sl, th), vh, vl);
-    fast_two_sum_(vh, __fadd_rn(tl, vl), zh, zl);
-    return df64(zh, zl);
+    df64 z;
+    D::add(x.hi, x.lo, y.hi, y.lo, z.hi, z.lo);
+    return z;
   }
   __device__ static df64 sub(df64 x, df64 y) { return add(x, df64(-y.hi, -y.lo)); }
   __device__ static df64 mul(df64 x, df64 y) {
-    const float ch = __fmul_rn(x.hi, y.hi);
-    const float cl1 = __fmaf_rn(x.hi, y.hi, -ch);
-    const float tl0 = __fmul_rn(x.lo, y.lo);
-    const float tl1 = __fmaf_rn(x.hi, y.lo, tl0);
-    const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
-    float zh, zl;
-    fast_two_sum_(ch, __fadd_rn(cl1, cl2), zh, zl);
-    return df64(zh, zl);
+    df64 z;
+    D::mul(x.hi, x.lo, y.hi, y.lo, z.hi, z.lo);
+    return z;
   }
   __device__ static df64 fma(df64 a, df64 b, df64 c) { return add(mul(a, b), c); }
+};
+
+template <> struct VA<df64x2> {
+  using S = double;
+  using D = DWops<float2>;
+  __device__ static df64x2 splat(double s) {
+    const float h = (float)s, l = (float)(s - (double)h);
+    return df64x2(make_float2(h, h), make_float2(l, l));
+  }
+  __device__ static df64x2 add(df64x2 x, df64x2 y) {
+    df64x2 z;
+    D::add(x.hi, x.lo, y.hi, y.lo, z.hi, z.lo);
+    return z;
+  }
+  __device__ static df64x2 sub(df64x2 x, df64x2 y) {
+    return add(x, df64x2(D::neg(y.hi), D::neg(y.lo)));
+  }
+  __device__ static df64x2 mul(df64x2 x, df64x2 y) {
+    df64x2 z;
+    D::mul(x.hi, x.lo, y.hi, y.lo, z.hi, z.lo);
+    return z;
+  }
+  __device__ static df64x2 fma(df64x2 a, df64x2 b, df64x2 c) { return add(mul(a, b), c); }
 };
 
 // acc + K v with K = NUM / DEN a power of two (1 and -1 without a product).
@@ -129,77 +175,193 @@ __device__ __forceinline__ V acc_(V acc, V v) {
   else return O::fma(v, O::splat(typename O::S(double(NUM) / double(DEN))), acc);
 }
 
-// BGK relaxation toward the incompressible equilibrium, written per +/- pair:
-// the pair shares (e.u)^2 and the even part of feq; the odd part flips sign.
-// f is in storage units (SF::scale): the weights carry the scale, which a pair
-// shares (opposite directions have the same weight).
-//   c0 = rho3 - 1.5 |u|^2
-//   feq_{i,j} = ws_i (c0 + 4.5 (e.u)^2) +- 3 ws_i (e.u),  ws_i = w_i scale_i
-//   f <- f + omega (feq - f)
+// Index of the direction with velocity (ex, ey, ez), -1 if none; and the
+// weight class of direction i (|e_i|^2: 0 rest, 1 axis, 2 face diagonal,
+// 3 corner).
+template <class L>
+__host__ __device__ constexpr int dir_of(int ex, int ey, int ez) {
+  for (int k = 0; k < L::Q; ++k)
+    if (L::ex(k) == ex && L::ey(k) == ey && L::ez(k) == ez) return k;
+  return -1;
+}
+template <class L>
+__host__ __device__ constexpr int wclass(int i) {
+  return L::ex(i) * L::ex(i) + L::ey(i) * L::ey(i) + L::ez(i) * L::ez(i);
+}
+// Pair index k (L::pair(k) = i) of direction i or of its opposite.
+template <class L>
+__host__ __device__ constexpr int pair_of(int i) {
+  for (int k = 0; k < L::NPAIR; ++k)
+    if (L::pair(k) == i || L::opp(L::pair(k)) == i) return k;
+  return -1;
+}
+
+// Relaxation constants of a sweep (SweepArgs::rk, host-computed per handle):
+//   rk[0]      = 1 - omega
+//   rk[1 + c]  = omega w_c s_c         (Kw, weight class c, storage scale s_c)
+//   rk[5 + c]  = 4.5 omega w_c s_c     (Ka)
+//   rk[9 + c]  = 3 omega w_c s_c       (K3)
+// in FP64 (rk), FP32 (rkf) and as the FP32 remainder rk - rkf (rkl), which
+// with rkf forms the double-float constant.
+constexpr int RK_OMC = 0, RK_W = 1, RK_A = 5, RK_3 = 9, RK_N = 13;
+template <class V> __device__ __forceinline__ V rconst(const SweepArgs &a, int k);
+template <> __device__ __forceinline__ double rconst<double>(const SweepArgs &a, int k) {
+  return a.rk[k];
+}
+template <> __device__ __forceinline__ float rconst<float>(const SweepArgs &a, int k) {
+  return a.rkf[k];
+}
+template <> __device__ __forceinline__ float2 rconst<float2>(const SweepArgs &a, int k) {
+  return make_float2(a.rkf[k], a.rkf[k]);
+}
+template <> __device__ __forceinline__ df64 rconst<df64>(const SweepArgs &a, int k) {
+  return df64(a.rkf[k], a.rkl[k]);
+}
+template <> __device__ __forceinline__ df64x2 rconst<df64x2>(const SweepArgs &a, int k) {
+  return df64x2(make_float2(a.rkf[k], a.rkf[k]), make_float2(a.rkl[k], a.rkl[k]));
+}
+
+// BGK relaxation toward the incompressible equilibrium
+//   feq_i = w_i (3p + 3 e_i.u + 4.5 (e_i.u)^2 - 1.5 |u|^2)
+// ("3D MPI+KOKKOS+MPIIO/lbm.cpp:257-272"), f <- (1 - omega) f + omega feq, with
+// omega and the weight folded into per-class constants (rconst) and written per
+// +/- pair: the pair shares e.u, (e.u)^2 and the even part of feq; the odd part
+// flips sign.  f is in storage units (SF::scale; the scale is folded into the
+// constants and a pair shares it).  Per cell and pair k of class c:
+//   c0 = rho3 - 1.5 |u|^2,  A_c = Kw_c c0,
+//   sym = Ka_c (e.u)^2 + A_c,  asym = K3_c e.u,
+//   f_i = (1 - omega) f_i + (sym + asym),  f_opp(i) = (1 - omega) f_opp(i) + (sym - asym).
+// The corner directions' e.u reuse the face diagonals' (e_x u_x + e_y u_y).
+// D3Q27 in FP64: 110 operations per cell (151 unfolded).
 template <class L, class V, class SF>
-__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, V om) {
+__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, const SweepArgs &a) {
   using O = VA<V>;
   using S = typename O::S;
-  const V usq = O::fma(ux, ux, O::fma(uy, uy, O::mul(uz, uz)));
+  const V omc = rconst<V>(a, RK_OMC);
+  V usq;
+  if constexpr (L::D == 3) usq = O::fma(ux, ux, O::fma(uy, uy, O::mul(uz, uz)));
+  else usq = O::fma(ux, ux, O::mul(uy, uy));
   const V c0 = O::fma(O::splat(S(-1.5)), usq, rho3);
-  f[0] = O::fma(om, O::sub(O::mul(O::splat(S(L::w(0) * SF::template scale<L>(0))), c0), f[0]),
-                f[0]);
+  constexpr int NC = L::D + 1;
+  V Ac[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) Ac[c] = O::mul(rconst<V>(a, RK_W + c), c0);
+  f[0] = O::fma(omc, f[0], Ac[0]);
+  V eu[L::NPAIR];
   static_for(
       [&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int i = L::pair(k), j = L::opp(L::pair(k));
-        constexpr double ws = L::w(i) * SF::template scale<L>(i);
         constexpr int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
-        // e.u with the components in x, y, z order
-        V eu;
-        if constexpr (ex != 0) {
-          eu = ex > 0 ? ux : O::sub(O::splat(S(0)), ux);
-          if constexpr (ey != 0) eu = ey > 0 ? O::add(eu, uy) : O::sub(eu, uy);
-          if constexpr (ez != 0) eu = ez > 0 ? O::add(eu, uz) : O::sub(eu, uz);
-        } else if constexpr (ey != 0) {
-          eu = ey > 0 ? uy : O::sub(O::splat(S(0)), uy);
-          if constexpr (ez != 0) eu = ez > 0 ? O::add(eu, uz) : O::sub(eu, uz);
+        constexpr int c = wclass<L>(i);
+        if constexpr (ex != 0 && ey != 0 && ez != 0) {
+          // corner: (e_x u_x + e_y u_y) of the face diagonal (e_x, e_y, 0), +- u_z
+          constexpr int kb = pair_of<L>(dir_of<L>(ex, ey, 0));
+          static_assert(kb >= 0 && kb < k, "face diagonal precedes the corner");
+          const V b = L::ex(L::pair(kb)) == ex ? eu[kb] : O::sub(O::splat(S(0)), eu[kb]);
+          eu[k] = ez > 0 ? O::add(b, uz) : O::sub(b, uz);
         } else {
-          eu = ez > 0 ? uz : O::sub(O::splat(S(0)), uz);
+          // sum of the nonzero signed components, led by a positive one
+          constexpr int n = (ex != 0) + (ey != 0) + (ez != 0);
+          const V cx = ux, cy = uy, cz = uz;
+          if constexpr (n == 1) {
+            eu[k] = ex > 0 ? cx : ex < 0 ? O::sub(O::splat(S(0)), cx)
+                  : ey > 0 ? cy : ey < 0 ? O::sub(O::splat(S(0)), cy)
+                  : ez > 0 ? cz : O::sub(O::splat(S(0)), cz);
+          } else {
+            // two components (p, q): the positive one first
+            constexpr bool hx = ex != 0, hy = ey != 0;
+            constexpr int s1 = hx ? ex : ey, s2 = hx ? (hy ? ey : ez) : ez;
+            const V p1 = hx ? cx : cy;
+            const V p2 = hx ? (hy ? cy : cz) : cz;
+            if constexpr (s1 > 0) eu[k] = s2 > 0 ? O::add(p1, p2) : O::sub(p1, p2);
+            else if constexpr (s2 > 0) eu[k] = O::sub(p2, p1);
+            else eu[k] = O::sub(O::sub(O::splat(S(0)), p1), p2);
+          }
         }
-        const V sym = O::mul(O::splat(S(ws)), O::fma(O::splat(S(4.5)), O::mul(eu, eu), c0));
-        const V asym = O::mul(O::splat(S(3.0 * ws)), eu);
-        f[i] = O::fma(om, O::sub(O::add(sym, asym), f[i]), f[i]);
-        f[j] = O::fma(om, O::sub(O::sub(sym, asym), f[j]), f[j]);
+        const V e2 = O::mul(eu[k], eu[k]);
+        const V sym = O::fma(e2, rconst<V>(a, RK_A + c), Ac[c]);
+        const V asym = O::mul(rconst<V>(a, RK_3 + c), eu[k]);
+        f[i] = O::fma(omc, f[i], O::add(sym, asym));
+        f[j] = O::fma(omc, f[j], O::sub(sym, asym));
       },
       std::make_integer_sequence<int, L::NPAIR>{});
 }
 
 template <class L, class A, class SF>
 __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const SweepArgs &a) {
-  A om;
-  if constexpr (sizeof(A) == 8) om = a.omega; else om = a.omega_f;
-  bgk_relax_v<L, A, SF>(f, rho3, ux, uy, uz, om);
+  bgk_relax_v<L, A, SF>(f, rho3, ux, uy, uz, a);
 }
 
-// Moments in deviation form: rho3 = 3p = sum f, u = sum f e, from populations
-// in storage units (the 1/scale factors are exact powers of two, 1 for FP32/64).
+// Moments in deviation form: rho3 = 3p = sum f, u = sum f e.
+// Unscaled storage (FP64, FP32): a three-level cascade over the 3 x 3 x 3 cube
+// of velocities -- per (e_x, e_y) line the sum and the difference along z, then
+// along y, then along x -- 49 additions for D3Q27 (14 for D2Q9) instead of 66
+// (18) with pair sums.  Scaled storage (FP16; the 1/scale factors are exact
+// powers of two that differ by weight class): pair sums and differences, each
+// scaled once.
 template <class L, class V, class SF>
 __device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
   using O = VA<V>;
   using S = typename O::S;
-  constexpr int S0 = (int)SF::template scale<L>(0);
-  if constexpr (S0 == 1) rho3 = f[0];
-  else rho3 = O::mul(f[0], O::splat(S(1.0 / S0)));
-  ux = uy = uz = O::splat(S(0));
-  static_for(
-      [&](auto kc) {
-        constexpr int k = decltype(kc)::value;
-        constexpr int i = L::pair(k), j = L::opp(L::pair(k));
-        constexpr int SC = (int)SF::template scale<L>(i);
-        const V sm = O::add(f[i], f[j]);
-        const V d = O::sub(f[i], f[j]);
-        rho3 = acc_<V, 1, SC>(rho3, sm);
-        if constexpr (L::ex(i) != 0) ux = acc_<V, L::ex(i), SC>(ux, d);
-        if constexpr (L::ey(i) != 0) uy = acc_<V, L::ey(i), SC>(uy, d);
-        if constexpr (L::ez(i) != 0) uz = acc_<V, L::ez(i), SC>(uz, d);
-      },
-      std::make_integer_sequence<int, L::NPAIR>{});
+  constexpr bool unscaled = SF::template scale<L>(0) == 1.0 && SF::template scale<L>(1) == 1.0 &&
+                            SF::template scale<L>(L::Q - 1) == 1.0;
+  if constexpr (unscaled && L::D == 3) {
+    V s0[3][3], s1[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const V lo = f[dir_of<L>(a - 1, b - 1, -1)];
+        const V mid = f[dir_of<L>(a - 1, b - 1, 0)];
+        const V hi = f[dir_of<L>(a - 1, b - 1, 1)];
+        s0[a][b] = O::add(O::add(lo, hi), mid);
+        s1[a][b] = O::sub(hi, lo);
+      }
+    V t00[3], t01[3], t10[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      t00[a] = O::add(O::add(s0[a][0], s0[a][2]), s0[a][1]);
+      t01[a] = O::sub(s0[a][2], s0[a][0]);
+      t10[a] = O::add(O::add(s1[a][0], s1[a][2]), s1[a][1]);
+    }
+    rho3 = O::add(O::add(t00[0], t00[2]), t00[1]);
+    ux = O::sub(t00[2], t00[0]);
+    uy = O::add(O::add(t01[0], t01[2]), t01[1]);
+    uz = O::add(O::add(t10[0], t10[2]), t10[1]);
+  } else if constexpr (unscaled) {
+    V s0[3], s1[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const V lo = f[dir_of<L>(a - 1, -1, 0)];
+      const V mid = f[dir_of<L>(a - 1, 0, 0)];
+      const V hi = f[dir_of<L>(a - 1, 1, 0)];
+      s0[a] = O::add(O::add(lo, hi), mid);
+      s1[a] = O::sub(hi, lo);
+    }
+    rho3 = O::add(O::add(s0[0], s0[2]), s0[1]);
+    ux = O::sub(s0[2], s0[0]);
+    uy = O::add(O::add(s1[0], s1[2]), s1[1]);
+    uz = O::splat(S(0));
+  } else {
+    constexpr int S0 = (int)SF::template scale<L>(0);
+    if constexpr (S0 == 1) rho3 = f[0];
+    else rho3 = O::mul(f[0], O::splat(S(1.0 / S0)));
+    ux = uy = uz = O::splat(S(0));
+    static_for(
+        [&](auto kc) {
+          constexpr int k = decltype(kc)::value;
+          constexpr int i = L::pair(k), j = L::opp(L::pair(k));
+          constexpr int SC = (int)SF::template scale<L>(i);
+          const V sm = O::add(f[i], f[j]);
+          const V d = O::sub(f[i], f[j]);
+          rho3 = acc_<V, 1, SC>(rho3, sm);
+          if constexpr (L::ex(i) != 0) ux = acc_<V, L::ex(i), SC>(ux, d);
+          if constexpr (L::ey(i) != 0) uy = acc_<V, L::ey(i), SC>(uy, d);
+          if constexpr (L::ez(i) != 0) uz = acc_<V, L::ez(i), SC>(uz, d);
+        },
+        std::make_integer_sequence<int, L::NPAIR>{});
+  }
 }
 
 // Macros out (when requested), Brinkman damping of the equilibrium velocity,
@@ -300,8 +462,35 @@ template <int Q, int I> struct DirC {
 // FP32 sweeps), in storage units (the host scales f_in / f_in_f).
 template <class A>
 __device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
-  if constexpr (sizeof(A) == 8) return a.f_in[i]; else return a.f_in_f[i];
+  if constexpr (std::is_same<A, df64>::value) return df64(a.f_in_f[i], a.f_in_l[i]);
+  else if constexpr (sizeof(A) == 8) return a.f_in[i];
+  else return a.f_in_f[i];
 }
+
+// Two cells per thread: the pair arithmetic type P (float2 or df64x2) and its
+// per-cell component type C (float or df64).
+template <class P> struct PairT;
+template <> struct PairT<float2> {
+  using C = float;
+  __device__ static float2 make(float a, float b) { return make_float2(a, b); }
+  __device__ static float x(float2 p) { return p.x; }
+  __device__ static float y(float2 p) { return p.y; }
+  __device__ static double to_double(float c) { return f2d_bits(c); }
+  __device__ static float third(float c) { return __fmul_rn(c, 1.0f / 3.0f); }
+};
+template <> struct PairT<df64x2> {
+  using C = df64;
+  __device__ static df64x2 make(df64 a, df64 b) {
+    return df64x2(make_float2(a.hi, b.hi), make_float2(a.lo, b.lo));
+  }
+  __device__ static df64 x(df64x2 p) { return df64(p.hi.x, p.lo.x); }
+  __device__ static df64 y(df64x2 p) { return df64(p.hi.y, p.lo.y); }
+  __device__ static double to_double(df64 c) { return (double)c; }
+  __device__ static double third_d(double d) { return __ddiv_rn(d, 3.0); }
+  __device__ static df64 third(df64 c) {
+    return VA<df64>::mul(c, VA<df64>::splat(1.0 / 3.0));
+  }
+};
 
 // Post-stream population I of cell X (offset c) for rows away from the y/z
 // faces and cells away from solids: the plain pull, with the inlet column
@@ -424,45 +613,48 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
 // arithmetic: a warp takes the two warp tiles 2b and 2b + 1 of a row, so a thread
 // owns cells x and x + 32, whose loads and stores share their address (the
 // second is an immediate 32 elements further).  Moments and BGK run once on
-// float2 values (FADD2/FMUL2/FFMA2), halving the arithmetic instructions of
-// the issue-bound FP32-collision forms.  A pair holding a listed tile pulls
-// through pull_pair_listed (face-state tables and link words).
-template <int Q, class ST, int I>
-__device__ __forceinline__ float2 pull_pair(const typename Store<ST>::elem *__restrict__ p,
-                                           const typename Store<ST>::elem *__restrict__ pm0,
-                                           const typename Store<ST>::elem *__restrict__ pm1,
-                                           long long S, long long rs, long long zs, bool act0,
-                                           bool act1, bool inlet0, const SweepArgs &a) {
+// the pair type P -- float2 (FP32 collision) or df64x2 (double-float
+// collision) -- with GB300's packed FFMA2/FADD2/FMUL2, halving the arithmetic
+// instructions of the issue-bound collision forms.  A pair holding a listed
+// tile pulls through pull_pair_listed (face-state tables and link words).
+template <int Q, class ST, class P, int I>
+__device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restrict__ p,
+                                       const typename Store<ST>::elem *__restrict__ pm0,
+                                       const typename Store<ST>::elem *__restrict__ pm1,
+                                       long long S, long long rs, long long zs, bool act0,
+                                       bool act1, bool inlet0, const SweepArgs &a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using Dd = DirC<Q, I>;
+  using C = typename PairT<P>::C;
   const long long off = I * S - (Dd::ex + Dd::ey * rs + Dd::ez * zs);
-  float v0 = 0.0f, v1 = 0.0f;
+  C v0 = C(0.0f), v1 = C(0.0f);
   if constexpr (Dd::ex < 0) {  // the outlet column repeats itself (pm = p - 1 there)
-    if (act0) v0 = SF::template load<float, L>(pm0 + off, I);
-    if (act1) v1 = SF::template load<float, L>(pm1 + off, I);
+    if (act0) v0 = SF::template load<C, L>(pm0 + off, I);
+    if (act1) v1 = SF::template load<C, L>(pm1 + off, I);
   } else {
-    if (act0) v0 = SF::template load<float, L>(p + off, I);
-    if (act1) v1 = SF::template load<float, L>(p + off + 32, I);
+    if (act0) v0 = SF::template load<C, L>(p + off, I);
+    if (act1) v1 = SF::template load<C, L>(p + off + 32, I);
   }
-  if constexpr (Dd::ex > 0) v0 = inlet0 ? a.f_in_f[I] : v0;
-  return make_float2(v0, v1);
+  if constexpr (Dd::ex > 0) v0 = inlet0 ? inlet_pop<C>(a, I) : v0;
+  return PairT<P>::make(v0, v1);
 }
 
 // The pair pull of a listed tile pair: pull_listed for cells x0 and x0 + 32
 // (l0 / l1 their link words), both loads issued.
-template <int Q, class ST, int I>
-__device__ __forceinline__ float2 pull_pair_listed(const typename Store<ST>::elem *__restrict__ p,
-                                                   long long S, long long off, bool wbb,
-                                                   unsigned l0, unsigned l1, bool act1,
-                                                   bool out0, bool out1, bool inlet0,
-                                                   const SweepArgs &a) {
+template <int Q, class ST, class P, int I>
+__device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__restrict__ p,
+                                              long long S, long long off, bool wbb,
+                                              unsigned l0, unsigned l1, bool act1,
+                                              bool out0, bool out1, bool inlet0,
+                                              const SweepArgs &a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using Dd = DirC<Q, I>;
+  using C = typename PairT<P>::C;
   if constexpr (I == 0) {
-    return make_float2(SF::template load<float, L>(p, 0),
-                       act1 ? SF::template load<float, L>(p + 32, 0) : 0.0f);
+    return PairT<P>::make(SF::template load<C, L>(p, 0),
+                          act1 ? SF::template load<C, L>(p + 32, 0) : C(0.0f));
   } else {
     const bool bb0 = wbb || ((l0 >> I) & 1u), bb1 = wbb || ((l1 >> I) & 1u);
     long long s0 = off, s1 = off + 32;
@@ -471,10 +663,10 @@ __device__ __forceinline__ float2 pull_pair_listed(const typename Store<ST>::ele
       s1 += out1 ? Dd::ex : 0;
     }
     constexpr long long OS = Dd::opp;
-    float v0 = SF::template load<float, L>(p + (bb0 ? OS * S : s0), I);
-    const float v1 = act1 ? SF::template load<float, L>(p + (bb1 ? OS * S + 32 : s1), I) : 0.0f;
-    if constexpr (Dd::ex > 0) v0 = (!bb0 && inlet0) ? a.f_in_f[I] : v0;
-    return make_float2(v0, v1);
+    C v0 = SF::template load<C, L>(p + (bb0 ? OS * S : s0), I);
+    const C v1 = act1 ? SF::template load<C, L>(p + (bb1 ? OS * S + 32 : s1), I) : C(0.0f);
+    if constexpr (Dd::ex > 0) v0 = (!bb0 && inlet0) ? inlet_pop<C>(a, I) : v0;
+    return PairT<P>::make(v0, v1);
   }
 }
 
@@ -483,14 +675,16 @@ __device__ __forceinline__ float2 pull_pair_listed(const typename Store<ST>::ele
 // LISTED: the pair holds a listed tile; both cells pull through the face-state
 // tables and their link words l0 / l1 (bit 31: solid cell), act0 = true and
 // act1 = the second tile exists.
-template <int Q, class ST, bool LISTED = false>
+template <int Q, class ST, class P, bool LISTED = false>
 __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y, int z,
                                                bool act0, bool act1, unsigned l0 = 0u,
                                                unsigned l1 = 0u) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
-  using O = VA<float2>;
+  using O = VA<P>;
+  using T = PairT<P>;
+  using C = typename T::C;
   const int nx = a.L.nx, ny = a.L.ny;
   const int x1 = x0 + 32;
   const bool st0 = act0 && x0 < nx, st1 = act1 && x1 < nx;
@@ -501,7 +695,7 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
   const E *__restrict__ pm0 = p - (x0 == nx - 1 ? 1 : 0);
   const E *__restrict__ pm1 = p + 32 - (x1 == nx - 1 ? 1 : 0);
   const bool inlet0 = x0 == 0;
-  float2 f[Q];
+  P f[Q];
   if constexpr (LISTED) {
     const int st = face_state(y, z, ny, a.L.nz);
     const long long *__restrict__ offs = a.face_off + st * Q;
@@ -509,56 +703,63 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
     static_for(
         [&](auto ic) {
           constexpr int I = decltype(ic)::value;
-          f[I] = pull_pair_listed<Q, ST, I>(p, S, offs[I], (wbb >> I) & 1u, l0, l1, act1,
-                                            x0 == nx - 1, x1 == nx - 1, inlet0, a);
+          f[I] = pull_pair_listed<Q, ST, P, I>(p, S, offs[I], (wbb >> I) & 1u, l0, l1, act1,
+                                               x0 == nx - 1, x1 == nx - 1, inlet0, a);
         },
         std::make_integer_sequence<int, Q>{});
   } else {
     static_for(
         [&](auto ic) {
           constexpr int I = decltype(ic)::value;
-          f[I] = pull_pair<Q, ST, I>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1, inlet0, a);
+          f[I] = pull_pair<Q, ST, P, I>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1, inlet0, a);
         },
         std::make_integer_sequence<int, Q>{});
   }
-  float2 rho3, ux, uy, uz;
-  moments<L, float2, SF>(f, rho3, ux, uy, uz);
+  P rho3, ux, uy, uz;
+  moments<L, P, SF>(f, rho3, ux, uy, uz);
   if constexpr (LISTED) {  // solid cells: p = u = 0
-    if (l0 >> 31) { rho3.x = 0.0f; ux.x = 0.0f; uy.x = 0.0f; uz.x = 0.0f; }
-    if (l1 >> 31) { rho3.y = 0.0f; ux.y = 0.0f; uy.y = 0.0f; uz.y = 0.0f; }
+    const C z0 = C(0.0f);
+    if (l0 >> 31) {
+      rho3 = T::make(z0, T::y(rho3)); ux = T::make(z0, T::y(ux));
+      uy = T::make(z0, T::y(uy)); uz = T::make(z0, T::y(uz));
+    }
+    if (l1 >> 31) {
+      rho3 = T::make(T::x(rho3), z0); ux = T::make(T::x(ux), z0);
+      uy = T::make(T::x(uy), z0); uz = T::make(T::x(uz), z0);
+    }
   }
   const long long cell0 = ((long long)z * ny + y) * nx + x0;
   if (a.mu) {
     if (st0) {
-      a.mu[cell0] = f2d_bits(ux.x);
-      a.mv[cell0] = f2d_bits(uy.x);
-      a.mw[cell0] = f2d_bits(uz.x);
-      a.mp[cell0] = f2d_bits(__fmul_rn(rho3.x, 1.0f / 3.0f));
+      a.mu[cell0] = T::to_double(T::x(ux));
+      a.mv[cell0] = T::to_double(T::x(uy));
+      a.mw[cell0] = T::to_double(T::x(uz));
+      a.mp[cell0] = T::to_double(T::third(T::x(rho3)));
     }
     if (st1) {
-      a.mu[cell0 + 32] = f2d_bits(ux.y);
-      a.mv[cell0 + 32] = f2d_bits(uy.y);
-      a.mw[cell0 + 32] = f2d_bits(uz.y);
-      a.mp[cell0 + 32] = f2d_bits(__fmul_rn(rho3.y, 1.0f / 3.0f));
+      a.mu[cell0 + 32] = T::to_double(T::y(ux));
+      a.mv[cell0 + 32] = T::to_double(T::y(uy));
+      a.mw[cell0 + 32] = T::to_double(T::y(uz));
+      a.mp[cell0 + 32] = T::to_double(T::third(T::y(rho3)));
     }
   }
   if (a.alpha) {
-    const float2 sb = make_float2(__fsub_rn(1.0f, st0 ? a.alpha[cell0] : 0.0f),
-                                  __fsub_rn(1.0f, st1 ? a.alpha[cell0 + 32] : 0.0f));
+    const P sb = T::make(C(__fsub_rn(1.0f, st0 ? a.alpha[cell0] : 0.0f)),
+                         C(__fsub_rn(1.0f, st1 ? a.alpha[cell0 + 32] : 0.0f)));
     ux = O::mul(ux, sb);
     uy = O::mul(uy, sb);
     uz = O::mul(uz, sb);
   }
-  bgk_relax_v<L, float2, SF>(f, rho3, ux, uy, uz, O::splat(a.omega_f));
+  bgk_relax_v<L, P, SF>(f, rho3, ux, uy, uz, a);
   E *__restrict__ q = static_cast<E *>(a.fb) + c;
 #pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    if (st0) SF::template store<float, L>(q + i * S, f[i].x, i);
-    if (st1) SF::template store<float, L>(q + i * S + 32, f[i].y, i);
+  for (int i = 0; i < L::Q; ++i) {
+    if (st0) SF::template store<C, L>(q + i * S, T::x(f[i]), i);
+    if (st1) SF::template store<C, L>(q + i * S + 32, T::y(f[i]), i);
   }
 }
 
-template <int Q, class ST, int MINB>
+template <int Q, class ST, class P, int MINB>
 __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
     sweep_channel2_kernel(const SweepArgs a) {
   const int ny = a.L.ny;
@@ -571,11 +772,11 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
   const int t1 = has1 ? a.tile_index[trow + w0 + 1] : -1;
   const int x0 = 32 * w0 + threadIdx.x;
   if (t0 < 0 && t1 < 0) {  // warp-uniform
-    channel2_cells<Q, ST>(a, x0, y, z, true, has1);
+    channel2_cells<Q, ST, P>(a, x0, y, z, true, has1);
   } else {
     const unsigned l0 = t0 >= 0 ? a.links_bits[(long long)t0 * SWEEP_BX + threadIdx.x] : 0u;
     const unsigned l1 = t1 >= 0 ? a.links_bits[(long long)t1 * SWEEP_BX + threadIdx.x] : 0u;
-    channel2_cells<Q, ST, true>(a, x0, y, z, true, has1, l0, l1);
+    channel2_cells<Q, ST, P, true>(a, x0, y, z, true, has1, l0, l1);
   }
 }
 
@@ -813,9 +1014,13 @@ void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) 
     bool wide = false;
     if constexpr (Q == 9) {
       wide = (long long)a.L.nx * a.L.ny * a.L.nz >= (1LL << 20);
-      if (wide) sweep_channel2_kernel<Q, ST, 10><<<g2, block, 0, s>>>(a);
+      if (wide) sweep_channel2_kernel<Q, ST, float2, 10><<<g2, block, 0, s>>>(a);
     }
-    if (!wide) sweep_channel2_kernel<Q, ST, M2><<<g2, block, 0, s>>>(a);
+    if (!wide) sweep_channel2_kernel<Q, ST, float2, M2><<<g2, block, 0, s>>>(a);
+  } else if constexpr (std::is_same<A, df64>::value) {
+    // Double-float collision on FP64 storage: two cells per thread on df64x2.
+    dim3 g2((a.nxw + 1) / 2, grid.y, grid.z);
+    sweep_channel2_kernel<Q, ST, df64x2, (Q == 27 ? 2 : 4)><<<g2, block, 0, s>>>(a);
   } else {
     sweep_channel_kernel<Q, ST, A, MINB_FAST><<<grid, block, 0, s>>>(a);
   }
