@@ -93,6 +93,8 @@ SIGNATURES = {
                              ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cflbm_mass": ([ctypes.c_void_p, _dp, _dp], ctypes.c_int),
     "cflbm_get_f": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "cflbm_get_f_stream": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "cflbm_get_solid": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8)], ctypes.c_int),
     "cflbm_set_f": ([ctypes.c_void_p, _dp, ctypes.c_int64], ctypes.c_int),
     "cflbm_get_info": ([ctypes.c_void_p, ctypes.POINTER(Info)], ctypes.c_int),
     "cflbm_write_tecplot": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),

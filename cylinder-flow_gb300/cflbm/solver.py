@@ -144,6 +144,19 @@ class Solver:
         C.check(C.lib.cflbm_get_f(self._h, _ptr(out)), "cflbm_get_f")
         return out
 
+    def get_f_stream(self):
+        """Post-stream (pre-collision) populations of the last step, shaped
+        (Q, nz, ny, nx): what the reference's f holds after Update."""
+        out = np.empty((self.Q,) + self.shape)
+        C.check(C.lib.cflbm_get_f_stream(self._h, _ptr(out)), "cflbm_get_f_stream")
+        return out
+
+    def solid(self):
+        """Interior solid mask (1 = solid), shaped (nz, ny, nx)."""
+        out = np.empty(self.shape, np.uint8)
+        C.check(C.lib.cflbm_get_solid(self._h, _ptr(out, ctypes.c_uint8)), "cflbm_get_solid")
+        return out
+
     def set_f(self, f, steps_done: int = 0):
         a = np.ascontiguousarray(f, np.float64).reshape((self.Q,) + self.shape)
         C.check(C.lib.cflbm_set_f(self._h, _ptr(a), int(steps_done)), "cflbm_set_f")

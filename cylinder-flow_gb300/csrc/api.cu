@@ -977,6 +977,38 @@ int cflbm_set_f(cflbm_handle *h, const double *in, int64_t steps_done) {
   return CFLBM_OK;
 }
 
+int cflbm_get_f_stream(cflbm_handle *h, double *out) {
+  if (!h || !out) return fail(CFLBM_E_INVALID, "bad arguments");
+  if (h->steps_done == 0) return cflbm_get_f(h, out);  // f = feq, as after Initialize
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t n = (size_t)h->Q * h->L.nx * h->L.ny * h->L.nz;
+  double *d = nullptr;
+  CK_CUDA(cudaMalloc(&d, n * sizeof(double)));
+  // fB: the state the last step pulled from (ghosts and solid nodes filled for
+  // the reference profiles); intact until the next step.
+  SweepArgs sa = channel_args(h, h->fB, nullptr, false);
+  cudaError_t e = launch_stream_state(h->Q, h->cfg.storage, sa,
+                                      h->cfg.profile != CFLBM_PROFILE_CHANNEL, d, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CK_CUDA(e);
+  return CFLBM_OK;
+}
+
+int cflbm_get_solid(cflbm_handle *h, uint8_t *out) {
+  if (!h || !out) return fail(CFLBM_E_INVALID, "bad arguments");
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  const int nx = h->L.nx, ny = h->L.ny, nz = h->L.nz;
+  std::vector<uint32_t> m((size_t)h->nxw * ny * nz);
+  CK_CUDA(cudaMemcpyAsync(m.data(), h->d_mask, m.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  for (long long r = 0; r < (long long)ny * nz; ++r)
+    for (int x = 0; x < nx; ++x)
+      out[(size_t)r * nx + x] = (m[(size_t)r * h->nxw + (x >> 5)] >> (x & 31)) & 1u;
+  return CFLBM_OK;
+}
+
 int cflbm_get_info(cflbm_handle *h, cflbm_info *info) {
   if (!h || !info) return fail(CFLBM_E_INVALID, "bad arguments");
   std::memset(info, 0, sizeof(*info));

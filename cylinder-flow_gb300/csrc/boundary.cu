@@ -486,6 +486,16 @@ cudaError_t launch_macros_channel(int Q, int store, int compute, const SweepArgs
                 : launch_macros_channel_q27(store, compute, a, s);
 }
 
+cudaError_t launch_stream_state_q9(int store, const SweepArgs &a, bool ref, double *out,
+                                   cudaStream_t s);
+cudaError_t launch_stream_state_q27(int store, const SweepArgs &a, bool ref, double *out,
+                                    cudaStream_t s);
+cudaError_t launch_stream_state(int Q, int store, const SweepArgs &a, bool ref, double *out,
+                                cudaStream_t s) {
+  return Q == 9 ? launch_stream_state_q9(store, a, ref, out, s)
+                : launch_stream_state_q27(store, a, ref, out, s);
+}
+
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
                                  cudaStream_t s, const SweepFork *fk) {
   return Q == 9 ? launch_sweep_channel_q9(store, compute, a, s, fk)

@@ -160,13 +160,6 @@ struct df64 {
   }
 };
 
-// Two cells' double-float numbers, component-wise (packed FP32x2 arithmetic).
-struct df64x2 {
-  float2 hi, lo;
-  df64x2() = default;
-  __device__ __forceinline__ df64x2(float2 h, float2 l) : hi(h), lo(l) {}
-};
-
 // Storage codecs.  load/store move values in "storage units": the population
 // times scale<L>(i) (1 for FP64 and FP32; the FP16 format's power of two), so
 // the FP16 path converts without a multiply; the sweep helpers fold 1/scale and

@@ -144,6 +144,10 @@ cudaError_t launch_macros_channel(int Q, int store, int compute, const SweepArgs
                                   cudaStream_t s);
 cudaError_t launch_sweep_channel(int Q, int store, int compute, const SweepArgs &a,
                                  cudaStream_t s, const SweepFork *fk = nullptr);
+// Post-stream populations of the step that read a.fa (FP64, dense [i][z][y][x]);
+// ref: plain pull (reference profiles), else the channel's resolved pull.
+cudaError_t launch_stream_state(int Q, int store, const SweepArgs &a, bool ref, double *out,
+                                cudaStream_t s);
 // Launch shape of the sweeps: blocks of 32 x 4 cells, one z plane per grid z
 // (the solid-tile launch runs 4 listed warp tiles per block).
 constexpr int SWEEP_BX = 32, SWEEP_BY = 4;

@@ -76,7 +76,7 @@ template <> struct VA<float2> {
   __device__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 };
 
-// Double-float arithmetic (df64 and its two-cell form df64x2, lattice.cuh)
+// Double-float arithmetic (df64, lattice.cuh)
 // from published error-free transformations: Knuth's TwoSum, Dekker's Fast2Sum
 // and the FMA-based exact product (Dekker, "A floating-point technique for
 // extending the available precision", Numer. Math. 18, 1971; Joldes, Muller and
@@ -90,8 +90,7 @@ template <> struct VA<float2> {
 //   mul: the exact product of the high parts plus the cross terms (the
 //        lo*lo term, ~u^2 of the product, dropped), Fast2Sum -- 8 operations;
 //        relative error <= 4u^2.
-// T = float (one cell) or float2 (two cells, GB300's packed FP32x2
-// instructions).
+// T = float (the df64 arithmetic of one cell per thread).
 template <class T> struct DWops {
   using O = VA<T>;
   __device__ static T neg(T a) { return O::sub(O::splat(0.0f), a); }
@@ -143,28 +142,6 @@ template <> struct VA<df64> {
   __device__ static df64 fma(df64 a, df64 b, df64 c) { return add(mul(a, b), c); }
 };
 
-template <> struct VA<df64x2> {
-  using S = double;
-  using D = DWops<float2>;
-  __device__ static df64x2 splat(double s) {
-    const float h = (float)s, l = (float)(s - (double)h);
-    return df64x2(make_float2(h, h), make_float2(l, l));
-  }
-  __device__ static df64x2 add(df64x2 x, df64x2 y) {
-    df64x2 z;
-    D::add(x.hi, x.lo, y.hi, y.lo, z.hi, z.lo);
-    return z;
-  }
-  __device__ static df64x2 sub(df64x2 x, df64x2 y) {
-    return add(x, df64x2(D::neg(y.hi), D::neg(y.lo)));
-  }
-  __device__ static df64x2 mul(df64x2 x, df64x2 y) {
-    df64x2 z;
-    D::mul(x.hi, x.lo, y.hi, y.lo, z.hi, z.lo);
-    return z;
-  }
-  __device__ static df64x2 fma(df64x2 a, df64x2 b, df64x2 c) { return add(mul(a, b), c); }
-};
 
 // acc + K v with K = NUM / DEN a power of two (1 and -1 without a product).
 template <class V, int NUM, int DEN>
@@ -217,9 +194,7 @@ template <> __device__ __forceinline__ float2 rconst<float2>(const SweepArgs &a,
 template <> __device__ __forceinline__ df64 rconst<df64>(const SweepArgs &a, int k) {
   return df64(a.rkf[k], a.rkl[k]);
 }
-template <> __device__ __forceinline__ df64x2 rconst<df64x2>(const SweepArgs &a, int k) {
-  return df64x2(make_float2(a.rkf[k], a.rkf[k]), make_float2(a.rkl[k], a.rkl[k]));
-}
+
 
 // BGK relaxation toward the incompressible equilibrium
 //   feq_i = w_i (3p + 3 e_i.u + 4.5 (e_i.u)^2 - 1.5 |u|^2)
@@ -467,8 +442,8 @@ __device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
   else return a.f_in_f[i];
 }
 
-// Two cells per thread: the pair arithmetic type P (float2 or df64x2) and its
-// per-cell component type C (float or df64).
+// Two cells per thread: the pair arithmetic type P (float2) and its per-cell
+// component type C (float).
 template <class P> struct PairT;
 template <> struct PairT<float2> {
   using C = float;
@@ -477,19 +452,6 @@ template <> struct PairT<float2> {
   __device__ static float y(float2 p) { return p.y; }
   __device__ static double to_double(float c) { return f2d_bits(c); }
   __device__ static float third(float c) { return __fmul_rn(c, 1.0f / 3.0f); }
-};
-template <> struct PairT<df64x2> {
-  using C = df64;
-  __device__ static df64x2 make(df64 a, df64 b) {
-    return df64x2(make_float2(a.hi, b.hi), make_float2(a.lo, b.lo));
-  }
-  __device__ static df64 x(df64x2 p) { return df64(p.hi.x, p.lo.x); }
-  __device__ static df64 y(df64x2 p) { return df64(p.hi.y, p.lo.y); }
-  __device__ static double to_double(df64 c) { return (double)c; }
-  __device__ static double third_d(double d) { return __ddiv_rn(d, 3.0); }
-  __device__ static df64 third(df64 c) {
-    return VA<df64>::mul(c, VA<df64>::splat(1.0 / 3.0));
-  }
 };
 
 // Post-stream population I of cell X (offset c) for rows away from the y/z
@@ -613,9 +575,11 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
 // arithmetic: a warp takes the two warp tiles 2b and 2b + 1 of a row, so a thread
 // owns cells x and x + 32, whose loads and stores share their address (the
 // second is an immediate 32 elements further).  Moments and BGK run once on
-// the pair type P -- float2 (FP32 collision) or df64x2 (double-float
-// collision) -- with GB300's packed FFMA2/FADD2/FMUL2, halving the arithmetic
-// instructions of the issue-bound collision forms.  A pair holding a listed
+// the pair type P = float2 with GB300's packed FFMA2/FADD2/FMUL2, halving the
+// arithmetic instructions of the issue-bound FP32-collision forms.  (A
+// double-float pair type needs ~250 registers for two cells' 27 populations;
+// at 2-3 blocks per SM it ran at 2.9-3.9 G cell updates/s against 7.5 for one
+// cell per thread at 5 blocks per SM, D3Q27 512x128x128.)  A pair holding a listed
 // tile pulls through pull_pair_listed (face-state tables and link words).
 template <int Q, class ST, class P, int I>
 __device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restrict__ p,
@@ -988,6 +952,55 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY) macros_channel_kernel(con
   if (valid) store_macros<A>(a, ((long long)z * ny + y) * nx + x, rho3, ux, uy, uz);
 }
 
+// The post-stream (pre-collision) populations of the step that read a.fa, in
+// FP64, dense [i][z][y][x] into out: what the reference's f holds after its
+// Streaming() and Update().  Channel profile: the step's resolved pull;
+// reference profiles: the plain pull from the ghost-filled state.
+template <int Q, class ST, bool REF>
+__global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY) stream_state_kernel(const SweepArgs a,
+                                                                           double *out) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx, ny = a.L.ny;
+  const int lane = threadIdx.x;
+  const int y = blockIdx.y * SWEEP_BY + threadIdx.y, z = blockIdx.z;
+  const int x = blockIdx.x * SWEEP_BX + lane;
+  if (y >= ny || x >= nx) return;
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  const long long N = (long long)nx * ny * a.L.nz;
+  const long long cell = ((long long)z * ny + y) * nx + x;
+  unsigned links = 0u;
+  if constexpr (!REF) {
+    const int t = a.tile_index[((long long)z * ny + y) * a.nxw + blockIdx.x];
+    links = t >= 0 ? a.links_bits[(long long)t * SWEEP_BX + lane] : 0u;
+  }
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        double v;
+        if constexpr (REF)
+          v = SF::template load<double, L>(fa + I * S + c - a.L.off(L::ex(I), L::ey(I), L::ez(I)),
+                                           I);
+        else
+          v = pull_resolved<Q, ST, double, I>(fa, c, S, x, y, z, links, a);
+        out[(long long)I * N + cell] = v / SF::template scale<L>(I);
+      },
+      std::make_integer_sequence<int, Q>{});
+}
+
+template <int Q, class ST>
+cudaError_t launch_stream_state_t(const SweepArgs &a, bool ref, double *out, cudaStream_t s) {
+  dim3 block(SWEEP_BX, SWEEP_BY, 1);
+  dim3 grid((a.L.nx + SWEEP_BX - 1) / SWEEP_BX, (a.L.ny + SWEEP_BY - 1) / SWEEP_BY, a.L.nz);
+  if (ref) stream_state_kernel<Q, ST, true><<<grid, block, 0, s>>>(a, out);
+  else stream_state_kernel<Q, ST, false><<<grid, block, 0, s>>>(a, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
 template <int Q, class ST, class A>
 cudaError_t launch_macros_channel_t(const SweepArgs &a, cudaStream_t s) {
   dim3 block(SWEEP_BX, SWEEP_BY, 1);
@@ -1017,10 +1030,6 @@ void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) 
       if (wide) sweep_channel2_kernel<Q, ST, float2, 10><<<g2, block, 0, s>>>(a);
     }
     if (!wide) sweep_channel2_kernel<Q, ST, float2, M2><<<g2, block, 0, s>>>(a);
-  } else if constexpr (std::is_same<A, df64>::value) {
-    // Double-float collision on FP64 storage: two cells per thread on df64x2.
-    dim3 g2((a.nxw + 1) / 2, grid.y, grid.z);
-    sweep_channel2_kernel<Q, ST, df64x2, (Q == 27 ? 2 : 4)><<<g2, block, 0, s>>>(a);
   } else {
     sweep_channel_kernel<Q, ST, A, MINB_FAST><<<grid, block, 0, s>>>(a);
   }

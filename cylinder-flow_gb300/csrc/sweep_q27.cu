@@ -26,10 +26,10 @@ cudaError_t launch_sweep_q27(int store, int compute, const SweepArgs &a, cudaStr
 
 cudaError_t launch_sweep_channel_q27(int store, int compute, const SweepArgs &a,
                                       cudaStream_t s, const SweepFork *fk) {
-  // Double-float channel sweep: 4 blocks per SM (128 registers; 3 / 4 / 5 per SM
-  // give 3,251 / 3,843 / 3,581 M cell updates/s at 512x128x128).
+  // Double-float channel sweep: 5 blocks per SM (102 registers; 3 / 4 / 5 / 6
+  // per SM give 6,839 / 6,972 / 7,468 / 7,434 M cell updates/s at 512x128x128).
   if (compute == COMPUTE_DF64)
-    return store == STORE_F64 ? launch_sweep_channel_t<27, double, df64, 4, 2>(a, s, fk)
+    return store == STORE_F64 ? launch_sweep_channel_t<27, double, df64, 5, 2>(a, s, fk)
                               : cudaErrorInvalidValue;
   if (compute == COMPUTE_F64) {
     switch (store) {
@@ -64,6 +64,16 @@ cudaError_t launch_macros_channel_q27(int store, int compute, const SweepArgs &a
       case STORE_F32: return launch_macros_channel_t<27, float, float>(a, s);
       case STORE_F16: return launch_macros_channel_t<27, F16Dev, float>(a, s);
     }
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_stream_state_q27(int store, const SweepArgs &a, bool ref, double *out,
+                                    cudaStream_t s) {
+  switch (store) {
+    case STORE_F64: return launch_stream_state_t<27, double>(a, ref, out, s);
+    case STORE_F32: return launch_stream_state_t<27, float>(a, ref, out, s);
+    case STORE_F16: return launch_stream_state_t<27, F16Dev>(a, ref, out, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -64,4 +64,14 @@ cudaError_t launch_macros_channel_q9(int store, int compute, const SweepArgs &a,
   return cudaErrorInvalidValue;
 }
 
+cudaError_t launch_stream_state_q9(int store, const SweepArgs &a, bool ref, double *out,
+                                    cudaStream_t s) {
+  switch (store) {
+    case STORE_F64: return launch_stream_state_t<9, double>(a, ref, out, s);
+    case STORE_F32: return launch_stream_state_t<9, float>(a, ref, out, s);
+    case STORE_F16: return launch_stream_state_t<9, F16Dev>(a, ref, out, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace cflbm

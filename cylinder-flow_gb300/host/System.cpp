@@ -1,6 +1,8 @@
 #include "System.hpp"
 
 #include <cmath>
+#include <initializer_list>
+#include <utility>
 #include <fstream>
 #include <iostream>
 #include <sstream>
@@ -25,6 +27,22 @@ void System::read(const std::string &path) {
   Time = std::pow(2 * R, 2) / miu;
   inter = Time / 10;
 
+  // Extension keys.  A value that names nothing known is an error (ok = false,
+  // `error` names the key): a misspelt profile or storage must not fall back
+  // to another solver silently.
+  auto pick = [&](const std::string &key, const std::string &v,
+                  std::initializer_list<std::pair<const char *, int>> names, int &dst) {
+    for (const auto &nv : names)
+      if (v == nv.first) {
+        dst = nv.second;
+        return;
+      }
+    std::string want;
+    for (const auto &nv : names) want += (want.empty() ? "" : ", ") + std::string(nv.first);
+    if (error.empty())
+      error = "input.in: cflbm." + key + " has unknown value '" + v + "' (expected one of " +
+              want + ")";
+  };
   std::string line;
   while (std::getline(input, line)) {
     std::istringstream ls(line);
@@ -32,6 +50,7 @@ void System::read(const std::string &path) {
     ls >> key;
     if (key.rfind("cflbm.", 0) != 0) continue;
     key = key.substr(6);
+    ext_keys.push_back(key);
     std::string v;
     if (key == "lattice") ls >> lattice;
     else if (key == "steps") ls >> Time;
@@ -40,26 +59,31 @@ void System::read(const std::string &path) {
     else if (key == "diam") ls >> diam;
     else if (key == "perturb") ls >> perturb;
     else if (key == "seed") ls >> seed;
-    else if (ls >> v) {
-      if (key == "profile")
-        profile = v == "channel" ? CFLBM_PROFILE_CHANNEL
-                  : v == "ref2d" ? CFLBM_PROFILE_REF2D : CFLBM_PROFILE_REF3D;
-      else if (key == "storage")
-        storage = v == "fp32" ? CFLBM_STORE_FP32 : v == "fp16dev" ? CFLBM_STORE_FP16DEV
-                                                                   : CFLBM_STORE_FP64;
-      else if (key == "compute")
-        compute = v == "fp32" ? CFLBM_COMPUTE_FP32 : v == "df64" ? CFLBM_COMPUTE_DF64
-                                                                 : CFLBM_COMPUTE_FP64;
-      else if (key == "geom")
-        geom = v == "cylinder" ? CFLBM_GEOM_CYLINDER : v == "sphere" ? CFLBM_GEOM_SPHERE
-                                                                      : CFLBM_GEOM_NONE;
-      else if (key == "wall_y" || key == "wall_z") {
-        int w = v == "noslip" ? CFLBM_WALL_NOSLIP : v == "periodic" ? CFLBM_WALL_PERIODIC
-                                                                    : CFLBM_WALL_FREESLIP;
-        (key == "wall_y" ? wall_y : wall_z) = w;
-      }
-    }
+    else if (!(ls >> v)) {
+      if (error.empty()) error = "input.in: cflbm." + key + " has no value";
+    } else if (key == "profile")
+      pick(key, v, {{"channel", CFLBM_PROFILE_CHANNEL}, {"ref2d", CFLBM_PROFILE_REF2D},
+                    {"ref3d", CFLBM_PROFILE_REF3D}}, profile);
+    else if (key == "storage")
+      pick(key, v, {{"fp64", CFLBM_STORE_FP64}, {"fp32", CFLBM_STORE_FP32},
+                    {"fp16dev", CFLBM_STORE_FP16DEV}}, storage);
+    else if (key == "compute")
+      pick(key, v, {{"fp64", CFLBM_COMPUTE_FP64}, {"fp32", CFLBM_COMPUTE_FP32},
+                    {"df64", CFLBM_COMPUTE_DF64}}, compute);
+    else if (key == "geom")
+      pick(key, v, {{"none", CFLBM_GEOM_NONE}, {"cylinder", CFLBM_GEOM_CYLINDER},
+                    {"sphere", CFLBM_GEOM_SPHERE}}, geom);
+    else if (key == "wall_y" || key == "wall_z")
+      pick(key, v, {{"freeslip", CFLBM_WALL_FREESLIP}, {"noslip", CFLBM_WALL_NOSLIP},
+                    {"periodic", CFLBM_WALL_PERIODIC}}, key == "wall_y" ? wall_y : wall_z);
+    else if (error.empty())
+      error = "input.in: unknown key cflbm." + key;
   }
+  if (lattice != CFLBM_D2Q9 && lattice != CFLBM_D3Q27 && error.empty())
+    error = "input.in: cflbm.lattice must be 9 or 27";
+  ext_error = !error.empty();
+  if (!error.empty()) ok = false;
+  else if (!ok) error = "could not read the nine numbers of " + path;
   if (inter <= 0) inter = 1;
 }
 

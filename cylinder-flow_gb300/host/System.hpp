@@ -11,11 +11,13 @@
 // solver options: lattice (9|27), profile (ref2d|ref3d|channel), storage
 // (fp64|fp32|fp16dev), compute (fp64|fp32|df64), steps (overrides the derived Time),
 // inter, geom (none|cylinder|sphere), center (cx cy cz), diam, wall_y, wall_z
-// (freeslip|noslip|periodic), perturb (amplitude), seed.
+// (freeslip|noslip|periodic), perturb (amplitude), seed.  An unknown key or
+// value sets ok = false and names it in `error`.
 #ifndef CFLBM_HOST_SYSTEM_HPP
 #define CFLBM_HOST_SYSTEM_HPP
 #include <cstdint>
 #include <string>
+#include <vector>
 
 class System {
  public:
@@ -40,6 +42,9 @@ class System {
   double perturb = 0.0;
   uint64_t seed = 1234;
   bool ok = false;  // input.in was found and parsed
+  std::string error;  // why not (an unreadable file, a bad extension key or value)
+  bool ext_error = false;             // `error` is about an extension key
+  std::vector<std::string> ext_keys;  // the extension keys the file set, in order
 
  private:
   void read(const std::string &path);

@@ -1,5 +1,7 @@
 #include "lbm.hpp"
 
+#include "System.hpp"
+
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -8,6 +10,28 @@
 #include <stdexcept>
 
 namespace {
+// The solver options that ./input.in's extension keys set (System.hpp), so the
+// reference's own main(), which passes only the grid, tau, rho0 and u0, can
+// select them too.  Keys the file does not set keep the constructor's defaults
+// (the reference's profile, FP64 storage and arithmetic); a bad key or value
+// throws.  No input.in: nothing changes.
+void apply_input_extensions(cflbm_config &c) {
+  System s("input.in");
+  if (s.ext_error) throw std::runtime_error(s.error);
+  for (const std::string &k : s.ext_keys) {
+    if (k == "profile") c.profile = s.profile;
+    else if (k == "storage") c.storage = s.storage;
+    else if (k == "compute") c.compute = s.compute;
+    else if (k == "geom") c.geom = s.geom;
+    else if (k == "center") { c.cx = s.cx; c.cy = s.cy; c.cz = s.cz; }
+    else if (k == "diam") c.diam = s.diam;
+    else if (k == "wall_y") c.wall_y = s.wall_y;
+    else if (k == "wall_z") c.wall_z = s.wall_z;
+    else if (k == "perturb") c.perturb_amp = s.perturb;
+    else if (k == "seed") c.seed = s.seed;
+  }
+}
+
 // The reference's ghost widths: 2 in 2-D ("MPI Kokkos/lbm.hpp:19"), 3 in 3-D
 // ("3D MPI+KOKKOS+MPIIO/lbm.hpp:22").
 int ghost_of(int dim) { return dim == 2 ? 2 : 3; }
@@ -15,7 +39,7 @@ int ghost_of(int dim) { return dim == 2 ? 2 : 3; }
 
 LBM::LBM(MPI_Comm comm_, int sx, int sy, int sz, double &tau, double &rho0_, double &u0_)
     : glx(sx), gly(sy), glz(sz), rho0(rho0_), tau0(tau), u0(u0_), dim(3),
-      ua(this, 0), va(this, 1), wa(this, 2), p(this, 3) {
+      ua(this, 0), va(this, 1), wa(this, 2), p(this, 3), f(this), usr(this), rho(this) {
   comm.comm = comm_;
   const int G = ghost_of(3);
   l_l[0] = sx;
@@ -37,11 +61,12 @@ LBM::LBM(MPI_Comm comm_, int sx, int sy, int sz, double &tau, double &rho0_, dou
   config.nx = sx;
   config.ny = sy;
   config.nz = sz;
+  apply_input_extensions(config);
 }
 
 LBM::LBM(MPI_Comm comm_, int sx, int sy, double &tau, double &rho0_, double &u0_)
     : glx(sx), gly(sy), glz(1), rho0(rho0_), tau0(tau), u0(u0_), dim(2),
-      ua(this, 0), va(this, 1), wa(this, 2), p(this, 3) {
+      ua(this, 0), va(this, 1), wa(this, 2), p(this, 3), f(this), usr(this), rho(this) {
   comm.comm = comm_;
   const int G = ghost_of(2);
   l_l[0] = sx;
@@ -62,6 +87,7 @@ LBM::LBM(MPI_Comm comm_, int sx, int sy, double &tau, double &rho0_, double &u0_
   config.nx = sx;
   config.ny = sy;
   config.nz = 1;
+  apply_input_extensions(config);
 }
 
 LBM::~LBM() {
@@ -84,6 +110,8 @@ void LBM::Initialize() {
   config.u0 = u0;
   check(cflbm_create(&config, &h_), "cflbm_create");
   fetched_step_ = -1;
+  pops_step_ = -1;
+  solid_.clear();
 }
 
 void LBM::Collision() {
@@ -116,6 +144,27 @@ const std::vector<double> &LBM::field(int which) {
   return f_[which];
 }
 
+const std::vector<double> &LBM::populations() {
+  flush_steps();
+  cflbm_info info;
+  check(cflbm_get_info(h_, &info), "cflbm_get_info");
+  if (pops_step_ != info.steps_done) {
+    pops_.resize((size_t)info.lattice * glx * gly * glz);
+    check(cflbm_get_f_stream(h_, pops_.data()), "cflbm_get_f_stream");
+    pops_step_ = info.steps_done;
+  }
+  return pops_;
+}
+
+const std::vector<uint8_t> &LBM::solid() {
+  if (solid_.empty()) {
+    if (!h_) throw std::runtime_error("LBM::usr before Initialize()");
+    solid_.resize((size_t)glx * gly * glz);
+    check(cflbm_get_solid(h_, solid_.data()), "cflbm_get_solid");
+  }
+  return solid_;
+}
+
 // "MPI Kokkos/lbm.cpp:398-407": every step appends "Cd Cl" (fixed, 17 digits)
 // to test.dat.  Kept on the GPU and appended in bulk here.
 void LBM::flush_forces() {
@@ -143,7 +192,8 @@ void LBM::MPIoutput(int n) {
 
 // The ASCII debugging dump ("MPI Kokkos/lbm.cpp:738-765", "3D.../lbm.cpp:741-771").
 // 2-D: x, y, u, v, p per node; 3-D: the node's integer coordinates and
-// population 1 of the stored (post-collision) state.
+// population 1 as the reference's f holds it after Update: the post-stream,
+// pre-collision value (the initial equilibrium at n = 0).
 void LBM::Output(int n) {
   flush_forces();
   std::ofstream out;
@@ -163,8 +213,7 @@ void LBM::Output(int n) {
       }
   } else {
     const size_t N = (size_t)glx * gly * glz;
-    std::vector<double> f(27 * N);
-    check(cflbm_get_f(h_, f.data()), "cflbm_get_f");
+    const std::vector<double> &f = populations();
     out << "variables=x,y,z,f" << std::endl;
     out << "zone I=" << lx - 6 << ",J=" << ly - 6 << ",K=" << lz - 6 << std::endl;
     for (int k = 0; k < glz; ++k)
@@ -197,3 +246,27 @@ double HostField::operator()(int i, int j, int k) const {
 
 const double *HostField::data() const { return owner_->field(which_).data(); }
 size_t HostField::size() const { return owner_->field(which_).size(); }
+
+double HostPops::operator()(int ii, int i, int j) const { return (*this)(ii, i, j, 0); }
+
+double HostPops::operator()(int ii, int i, int j, int k) const {
+  LBM *o = owner_;
+  const int G = o->l_s[0];
+  const int x = i - G, y = j - G, z = o->dim == 2 ? 0 : k - G;
+  if (x < 0 || x >= o->glx || y < 0 || y >= o->gly || z < 0 || z >= o->glz) return 0.0;
+  const size_t N = (size_t)o->glx * o->gly * o->glz;
+  return o->populations()[(size_t)ii * N + ((size_t)z * o->gly + y) * o->glx + x];
+}
+
+int HostUsr::operator()(int i, int j) const { return (*this)(i, j, owner_->l_s[0]); }
+
+int HostUsr::operator()(int i, int j, int k) const {
+  LBM *o = owner_;
+  const int G = o->l_s[0];
+  const int x = i - G, y = j - G, z = o->dim == 2 ? 0 : k - G;
+  if (x < 0 || x >= o->glx || y < 0 || y >= o->gly || z < 0 || z >= o->glz) return 1;
+  return o->solid()[((size_t)z * o->gly + y) * o->glx + x] ? 0 : 1;
+}
+
+double HostRho::operator()(int, int) const { return owner_->rho0; }
+double HostRho::operator()(int, int, int) const { return owner_->rho0; }

@@ -16,9 +16,19 @@
 // more; the 2-D per-step "Cd Cl" record of test.dat is kept on the GPU and
 // appended in bulk.
 //
+// The constructors apply the solver options that ./input.in's extension keys
+// set (System.hpp), so the reference's own main() selects them too; main()s
+// that set `config` themselves override them before Initialize().
+//
 // ua/va/wa/p are host views of the macroscopic fields with the reference's
 // ghost-inclusive indexing (ua(i,j,k) with i in [ghost, lx-ghost)); they are
-// refreshed from the GPU on first access after a step.
+// refreshed from the GPU on first access after a step.  f(ii,i,j,k) views the
+// populations as the reference's f holds them after Update -- the post-stream,
+// pre-collision state (cflbm_get_f_stream) -- usr(i,j,k) the solid mask (1 =
+// fluid, 0 = solid, "3D MPI+KOKKOS+MPIIO/lbm.cpp:238") and rho(i,j,k) the
+// density field, which the reference sets to rho0 in Initialize and never
+// updates (lbm.cpp:237; the flow's density is 1 + 3p).  Ghost nodes read as 0
+// (f, the macroscopic fields), 1 (usr) and rho0 (rho).
 #ifndef CFLBM_HOST_LBM_HPP
 #define CFLBM_HOST_LBM_HPP
 
@@ -28,12 +38,7 @@
 
 #include "../../include/cflbm.h"
 
-#ifndef MPI_VERSION
-typedef int MPI_Comm;
-#ifndef MPI_COMM_WORLD
-#define MPI_COMM_WORLD 0
-#endif
-#endif
+#include "mpi.h"  // the single-rank stand-in next to this header
 
 struct LBM;
 
@@ -51,6 +56,37 @@ class HostField {
   int which_;
 };
 
+// Host view of the populations (reference indexing f(ii, i, j[, k])).
+class HostPops {
+ public:
+  explicit HostPops(LBM *o) : owner_(o) {}
+  double operator()(int ii, int i, int j) const;
+  double operator()(int ii, int i, int j, int k) const;
+
+ private:
+  LBM *owner_;
+};
+
+// Host view of the reference's usr (1 = fluid, 0 = solid) and rho (rho0).
+class HostUsr {
+ public:
+  explicit HostUsr(LBM *o) : owner_(o) {}
+  int operator()(int i, int j) const;
+  int operator()(int i, int j, int k) const;
+
+ private:
+  LBM *owner_;
+};
+class HostRho {
+ public:
+  explicit HostRho(LBM *o) : owner_(o) {}
+  double operator()(int, int) const;
+  double operator()(int, int, int) const;
+
+ private:
+  LBM *owner_;
+};
+
 struct CommHelper {
   MPI_Comm comm = 0;
   int me = 0, nranks = 1;
@@ -66,6 +102,9 @@ struct LBM {
   double rho0, mu = 0, cs2 = 1.0 / 3.0, tau0, u0;
   int dim;
   HostField ua, va, wa, p;
+  HostPops f;
+  HostUsr usr;
+  HostRho rho;
 
   LBM(MPI_Comm comm_, int sx, int sy, int sz, double &tau, double &rho0_, double &u0_);
   LBM(MPI_Comm comm_, int sx, int sy, double &tau, double &rho0_, double &u0_);
@@ -94,6 +133,10 @@ struct LBM {
     return h_;
   }
   const std::vector<double> &field(int which);
+  // Post-stream populations of the last step, [ii][z][y][x] (cflbm_get_f_stream).
+  const std::vector<double> &populations();
+  // Interior solid mask, x fastest (cflbm_get_solid).
+  const std::vector<uint8_t> &solid();
 
  private:
   void check(int rc, const char *what);
@@ -103,8 +146,14 @@ struct LBM {
   int pending_ = 0;  // steps accounted for by Collision() and not yet run
   std::vector<double> f_[4];
   int64_t fetched_step_ = -1;
+  std::vector<double> pops_;
+  int64_t pops_step_ = -1;
+  std::vector<uint8_t> solid_;
   int64_t forces_flushed_ = 0;
   friend class HostField;
+  friend class HostPops;
+  friend class HostUsr;
+  friend class HostRho;
 };
 
 #endif

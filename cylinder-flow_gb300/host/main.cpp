@@ -11,7 +11,7 @@
 int main() {
   System s1;
   if (!s1.ok) {
-    std::fprintf(stderr, "could not read ./input.in\n");
+    std::fprintf(stderr, "%s\n", s1.error.c_str());
     return 2;
   }
   s1.Monitor();

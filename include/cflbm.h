@@ -167,6 +167,21 @@ int cflbm_mass(cflbm_handle *h, double *mass, double momentum[3]);
 int cflbm_get_f(cflbm_handle *h, double *out);
 int cflbm_set_f(cflbm_handle *h, const double *in, int64_t steps_done);
 
+/* The post-stream (pre-collision) populations of the last step in FP64, layout
+ * [i][z][y][x] (x fastest), q*nx*ny*nz doubles: what the reference's f holds
+ * after Streaming() and Update() ("3D MPI+KOKKOS+MPIIO/lbm.cpp:359-371",
+ * "MPI Kokkos/lbm.cpp:409-418", "Kokkos/lbm.cpp:178-186"), i.e. the state its Output() writes population 1 of
+ * ("3D MPI+KOKKOS+MPIIO/lbm.cpp:741-771").  Before the first step: the initial
+ * state, f = feq of the initial fields (as after LBM::Initialize).  The handle
+ * keeps the post-collision state; this forms the pull of the last step from the
+ * state that step read.  Synchronises. */
+int cflbm_get_f_stream(cflbm_handle *h, double *out);
+
+/* The interior solid mask, nx*ny*nz bytes (x fastest), 1 = solid: the
+ * complement of the reference's usr ("3D MPI+KOKKOS+MPIIO/lbm.cpp:238",
+ * usr = 1 in fluid).  Synchronises. */
+int cflbm_get_solid(cflbm_handle *h, uint8_t *out);
+
 /* Handle geometry, counters and memory. */
 int cflbm_get_info(cflbm_handle *h, cflbm_info *info);
 

@@ -180,6 +180,7 @@ int oracle_ref2d_run(int nx, int ny, double tau0, double u0, const int *ran, int
   };
 
   for (int it = 1; it <= steps; ++it) {
+    const double t_step = omp_get_wtime();
     collision();
     // Streaming, "MPI Kokkos/lbm.cpp:313-418".  Inlet copy (:315-321).
     for (int j = 1; j < ly - 1; ++j) {
@@ -348,6 +349,7 @@ int oracle_ref3d_run(int nx, int ny, int nz, double tau0, double u0, const int *
   };
 
   for (int it = 1; it <= steps; ++it) {
+    const double t_step = omp_get_wtime();
     collision();
     // Streaming ("3D MPI+KOKKOS+MPIIO/lbm.cpp:274-371"), face passes in the
     // reference's order: front (y lo), back (y hi), bottom (z lo), top (z hi),
@@ -520,7 +522,8 @@ int oracle_channel_mask(const oracle_channel_cfg *c, uint8_t *mask) {
 
 int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out,
                        double *u_out, double *v_out, double *w_out, double *p_out,
-                       double *force_out, int nthreads) {
+                       double *force_out, int nthreads, double *step_seconds,
+                       double *fstream_out) {
   if (nthreads > 0) omp_set_num_threads(nthreads);
   if (c->Q != 9 && c->Q != 27) return 1;
   const Lattice &L = (c->Q == 9) ? lat2() : lat3();
@@ -597,6 +600,7 @@ int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out
   };
 
   for (int it = 1; it <= steps; ++it) {
+    const double t_step = omp_get_wtime();
     collision();
     // Momentum exchange on fluid->solid links (post-collision state): every
     // pull of a fluid cell that bounces back off a solid source (after the
@@ -648,11 +652,13 @@ int oracle_channel_run(const oracle_channel_cfg *c, int steps, double *fpost_out
       va[n] = v * s;
       wa[n] = w * s;
     }
+    if (step_seconds) step_seconds[it - 1] = omp_get_wtime() - t_step;
   }
   if (u_out) std::memcpy(u_out, ua.data(), sizeof(double) * N);
   if (v_out) std::memcpy(v_out, va.data(), sizeof(double) * N);
   if (w_out) std::memcpy(w_out, wa.data(), sizeof(double) * N);
   if (p_out) std::memcpy(p_out, p.data(), sizeof(double) * N);
+  if (fstream_out) std::memcpy(fstream_out, f.data(), sizeof(double) * Q * N);
   if (fpost_out) {
     collision();
     std::memcpy(fpost_out, f.data(), sizeof(double) * Q * N);

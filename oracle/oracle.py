@@ -49,7 +49,7 @@ def lib():
                                        ctypes.c_double, ctypes.c_double, _ip, ctypes.c_int,
                                        _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]
         L.oracle_channel_run.argtypes = [ctypes.POINTER(ChannelCfg), ctypes.c_int, _dp, _dp,
-                                         _dp, _dp, _dp, _dp, ctypes.c_int]
+                                         _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.oracle_channel_mask.argtypes = [ctypes.POINTER(ChannelCfg),
                                           ctypes.POINTER(ctypes.c_uint8)]
         L.oracle_perturbation.argtypes = [ctypes.c_uint64, ctypes.c_long, ctypes.c_double]
@@ -118,19 +118,27 @@ def channel_cfg(Q, nx, ny, nz=1, tau0=0.03, u_in=0.05, wall_y=WALL_FREESLIP,
     return c
 
 
-def channel(cfg: ChannelCfg, steps: int, nthreads=0, want_f=True):
-    """Run the channel-profile oracle.  Arrays are interior only, x fastest."""
+def channel(cfg: ChannelCfg, steps: int, nthreads=0, want_f=True, want_fstream=False):
+    """Run the channel-profile oracle.  Arrays are interior only, x fastest;
+    ``fpost`` is the post-collision state after the run, ``fstream`` (on
+    request) the post-stream state the run ends with (the reference's f after
+    Update); ``step_seconds`` holds the wall time of every step
+    (initialisation excluded)."""
     nz = cfg.nz if cfg.Q == 27 else 1
     shp = (nz, cfg.ny, cfg.nx)
     out = dict(u=np.zeros(shp), v=np.zeros(shp), w=np.zeros(shp), p=np.zeros(shp),
-               force=np.zeros((max(steps, 1), 3)))
+               force=np.zeros((max(steps, 1), 3)), step_seconds=np.zeros(max(steps, 1)))
     if want_f:
         out["fpost"] = np.zeros((cfg.Q,) + shp)
+    if want_fstream:
+        out["fstream"] = np.zeros((cfg.Q,) + shp)
     rc = lib().oracle_channel_run(ctypes.byref(cfg), steps, _p(out.get("fpost")),
                                   _p(out["u"]), _p(out["v"]), _p(out["w"]), _p(out["p"]),
-                                  _p(out["force"]), nthreads)
+                                  _p(out["force"]), nthreads, _p(out["step_seconds"]),
+                                  _p(out.get("fstream")))
     assert rc == 0
     out["force"] = out["force"][:steps]
+    out["step_seconds"] = out["step_seconds"][:steps]
     return out
 
 

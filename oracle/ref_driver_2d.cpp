@@ -12,7 +12,8 @@
 // Writes into <outdir>: ran.i32 (lx*ly), f.f64 (9*lx*ly, post-stream, index
 // (ii*lx+i)*ly+j), fpost.f64 (same after one more Collision()), u.f64, v.f64,
 // p.f64 (lx*ly), test.dat (the reference's own per-step "Cd Cl" lines),
-// output0.plt / output1.plt (the reference's MPIoutput before and after the run).
+// output0.plt / output1.plt (the reference's MPIoutput before and after the run)
+// and output00.dat / output10.dat (its ASCII Output, before and after).
 #include <sys/stat.h>
 #include <unistd.h>
 #include <cstdio>
@@ -41,6 +42,8 @@ int main(int argc, char **argv) {
   std::remove("test.dat");
   std::remove("output0.plt");
   std::remove("output1.plt");
+  std::remove("output00.dat");
+  std::remove("output10.dat");
 
   MPI_Init(&argc, &argv);
   Kokkos::initialize(argc, argv);
@@ -49,6 +52,7 @@ int main(int argc, char **argv) {
     l1.Initialize();
     dump("ran.i32", l1.ran);
     l1.MPIoutput(0);
+    l1.Output(0);  // output00.dat: the initial state
     l1.setup_subdomain();
     for (int it = 1; it <= steps; ++it) {
       l1.Collision();
@@ -59,6 +63,7 @@ int main(int argc, char **argv) {
       l1.Update();
     }
     l1.MPIoutput(1);
+    l1.Output(1);  // output10.dat: after the run
     dump("f.f64", l1.f);
     dump("u.f64", l1.ua);
     dump("v.f64", l1.va);

@@ -11,7 +11,8 @@
 //   ref3d system <dir>        (constructs System from <dir>/input.in, prints it)
 //
 // "run" writes ran.i32, f.f64 (27*lx*ly*lz, index ((ii*lx+i)*ly+j)*lz+k),
-// fpost.f64, u.f64, v.f64, w.f64, p.f64, output0.plt and output1.plt.
+// fpost.f64, u.f64, v.f64, w.f64, p.f64, output0.plt and output1.plt (MPIoutput)
+// and output00.dat and output10.dat (the ASCII Output) before and after the run.
 #include <sys/stat.h>
 #include <unistd.h>
 #include <cstdio>
@@ -51,6 +52,8 @@ int main(int argc, char **argv) {
   int steps = std::atoi(argv[8]);
   std::remove("output0.plt");
   std::remove("output1.plt");
+  std::remove("output00.dat");
+  std::remove("output10.dat");
 
   MPI_Init(&argc, &argv);
   Kokkos::initialize(argc, argv);
@@ -59,12 +62,14 @@ int main(int argc, char **argv) {
     l1.Initialize();
     dump("ran.i32", l1.ran);
     l1.MPIoutput(0);
+    l1.Output(0);  // output00.dat: the initial state
     for (int it = 1; it <= steps; ++it) {
       l1.Collision();
       l1.Streaming();
       l1.Update();
     }
     l1.MPIoutput(1);
+    l1.Output(1);  // output10.dat: after the run
     dump("f.f64", l1.f);
     dump("u.f64", l1.ua);
     dump("v.f64", l1.va);

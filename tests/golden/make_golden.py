@@ -3,9 +3,10 @@
 Runs the reference's own sources (compiled unmodified against the Kokkos/MPI
 shim by oracle/build.py into oracle/_ref/) on small grids and stores what they
 produce: the per-node random draw, the post-collision populations and the
-macroscopic fields of the interior, the per-step "Cd Cl" lines of test.dat, the
-Tecplot files written by MPIoutput, and the parameters System derives from an
-input.in.  Needs the reference checkout; the fixtures are committed so the GPU
+macroscopic fields of the interior, the post-stream populations (the
+reference's f after Update), the per-step "Cd Cl" lines of test.dat, the
+Tecplot files written by MPIoutput, the ASCII files written by Output, and the
+parameters System derives from an input.in.  Needs the reference checkout; the fixtures are committed so the GPU
 box (which has no reference) can check against them.
 
     python tests/golden/make_golden.py
@@ -46,7 +47,13 @@ def main() -> None:
             meta=json.dumps(c), ran=r["ran"],
             # interior, transposed to x fastest: [.., y, x]
             fpost=r["fpost"][(slice(None),) + sl].transpose(0, 2, 1),
-            u=r["u"][sl].T, v=r["v"][sl].T, p=r["p"][sl].T, cdcl=cdcl)
+            u=r["u"][sl].T, v=r["v"][sl].T, p=r["p"][sl].T, cdcl=cdcl,
+            # the post-stream state after the run (the reference's f after Update)
+            fstream=r["f"][(slice(None),) + sl].transpose(0, 2, 1))
+        for k in (0, 1):
+            src = os.path.join(r["dir"], f"output{k}0.dat")
+            with open(src, "rb") as fh, open(os.path.join(HERE, f"{c['name']}_output{k}0.dat"), "wb") as out:
+                out.write(fh.read())
         for k in (0, 1):
             src = os.path.join(r["dir"], f"output{k}.plt")
             with open(src, "rb") as fh, open(os.path.join(HERE, f"{c['name']}_output{k}.plt"), "wb") as out:
@@ -60,7 +67,12 @@ def main() -> None:
             meta=json.dumps(c), ran=r["ran"],
             fpost=r["fpost"][(slice(None),) + sl].transpose(0, 3, 2, 1),
             u=r["u"][sl].transpose(2, 1, 0), v=r["v"][sl].transpose(2, 1, 0),
-            w=r["w"][sl].transpose(2, 1, 0), p=r["p"][sl].transpose(2, 1, 0))
+            w=r["w"][sl].transpose(2, 1, 0), p=r["p"][sl].transpose(2, 1, 0),
+            fstream=r["f"][(slice(None),) + sl].transpose(0, 3, 2, 1))
+        for k in (0, 1):
+            src = os.path.join(r["dir"], f"output{k}0.dat")
+            with open(src, "rb") as fh, open(os.path.join(HERE, f"{c['name']}_output{k}0.dat"), "wb") as out:
+                out.write(fh.read())
         src = os.path.join(r["dir"], "output1.plt")
         with open(src, "rb") as fh, open(os.path.join(HERE, f"{c['name']}_output1.plt"), "wb") as out:
             out.write(fh.read())

@@ -23,6 +23,7 @@ int main(int argc, char **argv) {
   std::printf("%d %d %d %d %d %.17g %.17g %.17g %.17g %d %d %.17g %llu\n", s.lattice,
               s.profile, s.storage, s.compute, s.geom, s.cx, s.cy, s.cz, s.diam, s.wall_y,
               s.wall_z, s.perturb, (unsigned long long)s.seed);
+  std::printf("%s\n", s.error.c_str());
   return 0;
 }
 '''
@@ -44,6 +45,11 @@ def read(exe, path):
     out = subprocess.run([exe, str(path)], capture_output=True, text=True,
                          check=True).stdout.split("\n")
     return out[0].split(), out[1].split()
+
+
+def read_error(exe, path):
+    return subprocess.run([exe, str(path)], capture_output=True, text=True,
+                          check=True).stdout.split("\n")[2]
 
 
 def test_derived_values_match_the_reference_system(system_exe, tmp_path):
@@ -86,3 +92,25 @@ def test_extension_key_selects_double_float_collision(system_exe, tmp_path):
                  "cflbm.compute df64\n")
     _, b = read(system_exe, p)
     assert b[1:4] == ["2", "0", "2"]  # profile REF3D, FP64 storage, double-float collision
+
+
+@pytest.mark.parametrize("key,value", [("profile", "Channel"), ("storage", "fp16"),
+                                       ("compute", "DF64"), ("geom", "disk"),
+                                       ("wall_y", "slip"), ("wall_z", "wall")])
+def test_unknown_extension_values_are_rejected(system_exe, tmp_path, key, value):
+    p = tmp_path / "input.in"
+    p.write_text("1.0  8.0  100\n0.05  100  10\n64  32  32\n=============\nrho R Re\n"
+                 f"cflbm.{key} {value}\n")
+    a, _ = read(system_exe, p)
+    assert a[0] == "0"
+    msg = read_error(system_exe, p)
+    assert f"cflbm.{key}" in msg and value in msg
+
+
+def test_unknown_extension_key_is_rejected(system_exe, tmp_path):
+    p = tmp_path / "input.in"
+    p.write_text("1.0  8.0  100\n0.05  100  10\n64  32  32\n=============\nrho R Re\n"
+                 "cflbm.storag fp32\n")
+    a, _ = read(system_exe, p)
+    assert a[0] == "0"
+    assert "cflbm.storag" in read_error(system_exe, p)

@@ -30,6 +30,7 @@ def test_ref2d_matches_reference_golden():
     sl = (slice(G, G + m["nx"]), slice(G, G + m["ny"]))
     # bit-for-bit: same expressions, same order, no contraction
     assert np.array_equal(o["fpost"][(slice(None),) + sl].transpose(0, 2, 1), g["fpost"])
+    assert np.array_equal(o["f"][(slice(None),) + sl].transpose(0, 2, 1), g["fstream"])
     assert np.array_equal(o["u"][sl].T, g["u"])
     assert np.array_equal(o["v"][sl].T, g["v"])
     assert np.array_equal(o["p"][sl].T, g["p"])
@@ -48,6 +49,7 @@ def test_ref3d_matches_reference_golden():
     G = 3
     sl = (slice(G, G + m["nx"]), slice(G, G + m["ny"]), slice(G, G + m["nz"]))
     assert np.array_equal(o["fpost"][(slice(None),) + sl].transpose(0, 3, 2, 1), g["fpost"])
+    assert np.array_equal(o["f"][(slice(None),) + sl].transpose(0, 3, 2, 1), g["fstream"])
     for k in ("u", "v", "w", "p"):
         assert np.array_equal(o[k][sl].transpose(2, 1, 0), g[k]), k
 
