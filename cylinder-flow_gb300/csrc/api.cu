@@ -64,7 +64,8 @@ void free_handle(cflbm_handle *h) {
                   h->d_links_bits, h->d_tile_slow, h->d_slow_tiles, h->d_tile_index,
                   h->d_face_off, h->d_face_bb,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
-                  h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums};
+                  h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums,
+                  h->d_err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
@@ -272,9 +273,10 @@ std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
   return flag;
 }
 
-// Equilibrium of the channel inlet (p = 0, u = (u_in, 0, 0)) in storage format.
+// Equilibrium of the channel inlet (p = 0, u = (u_in, 0, 0)) in storage format
+// (FP16: the deviation from the storage offset fbase, times F16_SCALE).
 template <int Q>
-std::vector<unsigned char> inlet_elements(double u_in, int storage) {
+std::vector<unsigned char> inlet_elements(double u_in, int storage, const float *fbase) {
   using L = Lat<Q>;
   std::vector<unsigned char> out((size_t)Q * store_size(storage));
   for (int i = 0; i < Q; ++i) {
@@ -286,11 +288,25 @@ std::vector<unsigned char> inlet_elements(double u_in, int storage) {
       const float v = (float)feq;
       std::memcpy(&out[4 * i], &v, 4);
     } else {
-      const __half v = __float2half_rn((float)(feq * (double)L::h_scale(i)));
+      const __half v = __double2half((feq - (double)fbase[i]) * (double)F16_SCALE);
       std::memcpy(&out[2 * i], &v, 2);
     }
   }
   return out;
+}
+
+// Storage offsets of the FP16 format: the free-stream equilibrium
+// feq_i(rho = 1, u = (u_ref, 0, 0)) in deviation form, rounded to FP32
+// (Store<F16Dev>); zero for the other formats.
+template <int Q>
+void storage_offsets(int storage, double u_ref, float *fbase) {
+  using L = Lat<Q>;
+  for (int i = 0; i < 27; ++i) fbase[i] = 0.0f;
+  if (storage != CFLBM_STORE_FP16DEV) return;
+  for (int i = 0; i < Q; ++i) {
+    const double edu = L::ex(i) * u_ref;
+    fbase[i] = (float)(L::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * u_ref * u_ref));
+  }
 }
 
 int validate(const cflbm_config *c) {
@@ -415,6 +431,11 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   }
   L.zs = L.rs * L.nyp;
   L.total = (long long)Q * L.px * L.nyp * L.nzp;
+  // FP16: the channel's free stream is the inlet's; the reference profiles'
+  // Poiseuille inlet has no single stream velocity, so they store f itself.
+  const double u_ref = cfg->profile == CFLBM_PROFILE_CHANNEL ? cfg->u0 : 0.0;
+  if (d3) storage_offsets<27>(cfg->storage, u_ref, L.fbase);
+  else storage_offsets<9>(cfg->storage, u_ref, L.fbase);
   h->nxw = (nx + 31) / 32;
   h->omega = 1.0 / (cfg->tau0 + 0.5);
   if (!(h->omega > 0.0 && h->omega < 2.0))
@@ -520,10 +541,16 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(unsigned), h->stream));
   CK_CUDA(cudaMemsetAsync(h->d_counter2, 0, sizeof(unsigned), h->stream));
   if ((rc = dev_alloc_t(h, &h->d_sums, 4))) return rc;
+  if ((rc = dev_alloc_t(h, &h->d_err, 1))) return rc;
+  CK_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream));
+  h->lines = cfg->profile == CFLBM_PROFILE_CHANNEL &&
+             lines_supported(Q, cfg->storage, cfg->layout == CFLBM_LAYOUT_ROWS,
+                             cfg->alpha != nullptr, nx);
+  if (h->lines) CK_CUDA(lines_prepare());
 
   if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
-    std::vector<unsigned char> fin = d3 ? inlet_elements<27>(cfg->u0, cfg->storage)
-                                        : inlet_elements<9>(cfg->u0, cfg->storage);
+    std::vector<unsigned char> fin = d3 ? inlet_elements<27>(cfg->u0, cfg->storage, L.fbase)
+                                        : inlet_elements<9>(cfg->u0, cfg->storage, L.fbase);
     if ((rc = dev_alloc(h, &h->d_fin, fin.size()))) return rc;
     CK_CUDA(cudaMemcpyAsync(h->d_fin, fin.data(), fin.size(), cudaMemcpyHostToDevice, h->stream));
     if (cfg->alpha) {
@@ -601,12 +628,12 @@ static int record_event(cflbm_handle *h, size_t *idx) {
 
 extern "C++" {
 namespace cflbm {
-void set_relax(SweepArgs &a, int Q, int store, double omega) {
+void set_relax(SweepArgs &a, int Q, int, double omega) {
   a.omega = omega;
   a.omega_f = (float)omega;
   double rk[13] = {1.0 - omega};
   for (int c = 0; c <= (Q == 27 ? 3 : 2); ++c) {
-    // weight and FP16 scale of class c (|e|^2 = c): the first direction of it
+    // weight of class c (|e|^2 = c): the first direction of it
     int i = 0;
     for (int k = 0; k < Q; ++k) {
       const int ex = Q == 27 ? Lat<27>::ex(k) : Lat<9>::ex(k);
@@ -614,11 +641,7 @@ void set_relax(SweepArgs &a, int Q, int store, double omega) {
       const int ez = Q == 27 ? Lat<27>::ez(k) : 0;
       if (ex * ex + ey * ey + ez * ez == c) { i = k; break; }
     }
-    const double w = Q == 27 ? Lat<27>::w(i) : Lat<9>::w(i);
-    const double sc = store != CFLBM_STORE_FP16DEV
-                          ? 1.0
-                          : (Q == 27 ? (double)Lat<27>::h_scale(i) : (double)Lat<9>::h_scale(i));
-    const double kw = omega * w * sc;
+    const double kw = omega * (Q == 27 ? Lat<27>::w(i) : Lat<9>::w(i));
     rk[1 + c] = kw;
     rk[5 + c] = 4.5 * kw;
     rk[9 + c] = 3.0 * kw;
@@ -648,14 +671,11 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   }
   sa.wall_y = h->cfg.wall_y;
   sa.wall_z = h->cfg.wall_z;
-  // Inlet populations in storage units (the FP16 format's power-of-two scale).
+  // Inlet populations in every arithmetic type.
   for (int i = 0; i < h->Q; ++i) {
-    const double sc = h->cfg.storage != CFLBM_STORE_FP16DEV
-                          ? 1.0
-                          : (h->Q == 27 ? (double)Lat<27>::h_scale(i) : (double)Lat<9>::h_scale(i));
-    sa.f_in[i] = h->f_in[i] * sc;
-    sa.f_in_f[i] = (float)(h->f_in[i] * sc);
-    sa.f_in_l[i] = (float)(h->f_in[i] * sc - (double)sa.f_in_f[i]);
+    sa.f_in[i] = h->f_in[i];
+    sa.f_in_f[i] = (float)h->f_in[i];
+    sa.f_in_l[i] = (float)(h->f_in[i] - (double)sa.f_in_f[i]);
   }
   // Persistent grid of the force launch beside the sweep: one block per SM
   // (measured on the D3Q27 512x128x128 bench step: 1 / 2 / 4 per SM give FP32
@@ -676,6 +696,9 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   sa.hist = h->d_hist;
   sa.step = h->d_step;
   sa.cap = h->hist_cap;
+  sa.sms = h->sms;
+  sa.lines = h->lines ? 1 : 0;
+  sa.err = h->d_err;
   return sa;
 }
 }  // namespace cflbm
@@ -815,12 +838,21 @@ int cflbm_step(cflbm_handle *h, int nsteps) {
   return CFLBM_OK;
 }
 
+// The device error word: a kernel whose bounded wait gave up recorded it.
+static int check_device_error(cflbm_handle *h) {
+  unsigned e = 0;
+  CK_CUDA(cudaMemcpyAsync(&e, h->d_err, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+  CK_CUDA(cudaStreamSynchronize(h->stream));
+  if (e) return fail(CFLBM_E_CUDA, "a sweep kernel's wait for its copies timed out (0x%08x)", e);
+  return CFLBM_OK;
+}
+
 int cflbm_synchronize(cflbm_handle *h) {
   if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
   CK_CUDA(cudaSetDevice(h->cfg.device));
   CK_CUDA(cudaStreamSynchronize(h->stream));
   CK_CUDA(cudaGetLastError());
-  return CFLBM_OK;
+  return check_device_error(h);
 }
 
 // Channel profile: forms u, v, w, p of the last step from the state that step
@@ -935,6 +967,7 @@ int cflbm_mass(cflbm_handle *h, double *mass, double momentum[3]) {
   double s[4];
   CK_CUDA(cudaMemcpyAsync(s, h->d_sums, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
   CK_CUDA(cudaStreamSynchronize(h->stream));
+  if (int rc = check_device_error(h)) return rc;
   if (!std::isfinite(s[0])) return fail(CFLBM_E_NUMERIC, "mass is not finite (%g)", s[0]);
   if (mass) *mass = s[0];
   if (momentum) {

@@ -47,21 +47,27 @@ template <int Q> __device__ int dmirror(int i, int d) {
   return i;
 }
 
+// FP64 values of stored elements and back (Store<> codecs; L.fbase is the
+// FP16 format's storage offset per population).
 template <class ST> struct Dec;
 template <> struct Dec<double> {
-  template <int Q> __device__ static double get(double v, int) { return v; }
-  template <int Q> __device__ static double put(double v, int) { return v; }
+  template <int Q> __device__ static double get(double v, int, const Layout &) { return v; }
+  template <int Q> __device__ static double put(double v, int, const Layout &) { return v; }
 };
 template <> struct Dec<float> {
-  template <int Q> __device__ static double get(float v, int) { return (double)v; }
-  template <int Q> __device__ static float put(double v, int) { return (float)v; }
+  template <int Q> __device__ static double get(float v, int, const Layout &) {
+    return (double)v;
+  }
+  template <int Q> __device__ static float put(double v, int, const Layout &) {
+    return (float)v;
+  }
 };
 template <> struct Dec<F16Dev> {
-  template <int Q> __device__ static double get(__half v, int i) {
-    return (double)__half2float(v) / (double)Lat<Q>::h_scale(i);
+  template <int Q> __device__ static double get(__half v, int i, const Layout &L) {
+    return __fma_rn((double)__half2float(v), 1.0 / F16_SCALE, (double)L.fbase[i]);
   }
-  template <int Q> __device__ static __half put(double v, int i) {
-    return __float2half_rn((float)(v * (double)Lat<Q>::h_scale(i)));
+  template <int Q> __device__ static __half put(double v, int i, const Layout &L) {
+    return __double2half(__dmul_rn(__dsub_rn(v, (double)L.fbase[i]), (double)F16_SCALE));
   }
 };
 
@@ -260,8 +266,8 @@ __global__ void links_kernel(const LinkArgs a) {
     const long long s = L.idx(l.x, l.y, l.z);
     const E v = f[kb * L.S + s + a.reach * ok];
     f[k * L.S + s] = v;
-    const double m = Dec<ST>::template get<Q>(f[kb * L.S + s + ok], kb) +
-                     Dec<ST>::template get<Q>(v, kb);
+    const double m = Dec<ST>::template get<Q>(f[kb * L.S + s + ok], kb, L) +
+                     Dec<ST>::template get<Q>(v, kb, L);
     fx += m * DT<Q>::ex(kb);
     fy += m * DT<Q>::ey(kb);
     fz += m * DT<Q>::ez(kb);
@@ -323,7 +329,7 @@ __global__ void init_macros_kernel(const Layout L, void *f_, const double *u, co
       const double udu = uu * uu + vv * vv + ww * ww;
       const double feq =
           Lat<Q>::w(i) * pp * 3.0 + Lat<Q>::w(i) * (3.0 * edu + 4.5 * edu * edu - 1.5 * udu);
-      f[i * L.S + c] = Dec<ST>::template put<Q>(feq, i);
+      f[i * L.S + c] = Dec<ST>::template put<Q>(feq, i, L);
     }
   }
 }
@@ -366,7 +372,7 @@ __global__ void init_channel_kernel(const Layout L, void *f_, const uint32_t *ma
                           Lat<Q>::w(i) * (3.0 * eb + 4.5 * eb * eb - 1.5 * ub);
         fp = f0 - (f0 - fb) * omega;
       }
-      f[i * L.S + c] = Dec<ST>::template put<Q>(fp, i);
+      f[i * L.S + c] = Dec<ST>::template put<Q>(fp, i, L);
     }
   }
 }
@@ -388,7 +394,7 @@ __global__ void reduce_mass_kernel(const ReduceArgs a) {
     const long long c = L.idx(x, y, z);
     double r = 1.0;
     for (int i = 0; i < Q; ++i) {
-      const double fi = Dec<ST>::template get<Q>(f[i * L.S + c], i);
+      const double fi = Dec<ST>::template get<Q>(f[i * L.S + c], i, L);
       r += fi;
       acc[1] += fi * DT<Q>::ex(i);
       acc[2] += fi * DT<Q>::ey(i);
@@ -439,7 +445,7 @@ __global__ void get_f_kernel(const Layout L, const void *f_, double *out) {
     const int x = (int)(n % L.nx);
     const int y = (int)((n / L.nx) % L.ny);
     const int z = (int)(n / ((long long)L.nx * L.ny));
-    out[t] = Dec<ST>::template get<Q>(f[i * L.S + L.idx(x, y, z)], i);
+    out[t] = Dec<ST>::template get<Q>(f[i * L.S + L.idx(x, y, z)], i, L);
   }
 }
 
@@ -455,7 +461,7 @@ __global__ void set_f_kernel(const Layout L, void *f_, const double *in) {
     const int x = (int)(n % L.nx);
     const int y = (int)((n / L.nx) % L.ny);
     const int z = (int)(n / ((long long)L.nx * L.ny));
-    f[i * L.S + L.idx(x, y, z)] = Dec<ST>::template put<Q>(in[t], i);
+    f[i * L.S + L.idx(x, y, z)] = Dec<ST>::template put<Q>(in[t], i, L);
   }
 }
 

@@ -48,6 +48,8 @@ struct cflbm_handle {
   unsigned int *d_counter = nullptr;   // links kernel
   unsigned int *d_counter2 = nullptr;  // mass kernel
   double *d_sums = nullptr;            // 4 doubles (mass, momentum)
+  unsigned *d_err = nullptr;           // device error word (a bounded wait gave up)
+  bool lines = false;                  // the interior runs the line-staged sweep
   long long steps_done = 0;
   double omega = 1.0;
   double area = 1.0;  // Cd/Cl reference area

@@ -37,7 +37,8 @@ template <> struct Lat<9> {
     constexpr int v[4] = {1, 2, 5, 6};
     return v[k];
   }
-  // Power-of-two scale close to 1/w_i used by the FP16 deviation format.
+  // Power-of-two scale close to 1/w_i: the FP16 format of the allocation-free
+  // domain sums (noalloc.cu) stores f_i times it.
   __host__ __device__ static constexpr float h_scale(int i) {
     return i == 0 ? 2.0f : (i < 5 ? 8.0f : 32.0f);
   }
@@ -88,7 +89,7 @@ __host__ __device__ constexpr int mirror(int i, int d) {
 
 // ---- storage formats ---------------------------------------------------------
 // Store<T>::load/store convert between the stored element and the arithmetic
-// type A; FP16 deviation storage keeps f_i * h_scale(i) in binary16.
+// type A; FP16 deviation storage is described at Store<F16Dev>.
 struct F16Dev {
   __half h;
 };
@@ -160,21 +161,26 @@ struct df64 {
   }
 };
 
-// Storage codecs.  load/store move values in "storage units": the population
-// times scale<L>(i) (1 for FP64 and FP32; the FP16 format's power of two), so
-// the FP16 path converts without a multiply; the sweep helpers fold 1/scale and
-// scale into their constants (moments, cell_force, bgk_relax, inlet values).
+// Storage codecs: load/store (global memory) and decode (an element already
+// read, e.g. from shared memory) convert between the stored element and the
+// arithmetic type A, so the arithmetic always sees the population itself.
+// `base` is the storage offset of the population (Layout::fbase): 0 for FP64 and
+// FP32; for FP16 deviation storage the equilibrium the format stores the
+// deviation from (see F16Dev).
 template <> struct Store<double> {
   using elem = double;
-  template <class L>
-  __host__ __device__ static constexpr double scale(int) { return 1.0; }
+  template <class A>
+  __device__ static A decode(elem v, float) {
+    if constexpr (sizeof(A) == 4) return d2f_bits(v);
+    else return static_cast<A>(v);
+  }
   template <class A, class L>
-  __device__ static A load(const elem *p, int) {
+  __device__ static A load(const elem *p, float) {
     if constexpr (sizeof(A) == 4) return d2f_bits(__ldg(p));
     else return static_cast<A>(__ldg(p));
   }
   template <class A, class L>
-  __device__ static void store(elem *p, A v, int) {
+  __device__ static void store(elem *p, A v, float) {
     if constexpr (sizeof(A) == 4) *p = f2d_bits(v);
     else *p = static_cast<double>(v);
   }
@@ -182,25 +188,44 @@ template <> struct Store<double> {
 
 template <> struct Store<float> {
   using elem = float;
-  template <class L>
-  __host__ __device__ static constexpr double scale(int) { return 1.0; }
+  template <class A>
+  __device__ static A decode(elem v, float) { return static_cast<A>(v); }
   template <class A, class L>
-  __device__ static A load(const elem *p, int) { return static_cast<A>(__ldg(p)); }
+  __device__ static A load(const elem *p, float) { return static_cast<A>(__ldg(p)); }
   template <class A, class L>
-  __device__ static void store(elem *p, A v, int) { *p = static_cast<float>(v); }
+  __device__ static void store(elem *p, A v, float) { *p = static_cast<float>(v); }
 };
 
+// FP16 deviation storage: binary16 of (f_i - base_i) * 2^F16_EXP.  f_i is the
+// reference's deviation form already (f_i - w_i rho0); base_i is the
+// equilibrium of the free stream, feq_i(rho = 1, u = (u_ref, 0, 0)) (u_ref =
+// the inlet speed of a channel, 0 for the reference profiles), so cells of the
+// undisturbed stream store values near zero and keep binary16's relative
+// precision on what differs from the free stream (the shifted-distribution
+// idea of Lehmann et al., Phys. Rev. E 106, 015308, 2022, taken one step
+// further).  One power of two for every direction: binary16 holds 2^-14..2^16
+// normal, |f - base| stays below 0.1 in any flow the lattice can represent, so
+// 2^12 keeps every value above 2^-24/2^12 normal down to 1.5e-8 with room to
+// spare.  Decode: one FMA (the product by 2^-12 is exact); encode: subtract,
+// scale, round to nearest.
+constexpr float F16_SCALE = 4096.0f;
 template <> struct Store<F16Dev> {
   using elem = __half;
-  template <class L>
-  __host__ __device__ static constexpr double scale(int i) { return L::h_scale(i); }
-  template <class A, class L>
-  __device__ static A load(const elem *p, int) {
-    return static_cast<A>(__half2float(__ldg(p)));
+  template <class A>
+  __device__ static A decode(elem v, float base) {
+    const float h = __half2float(v);
+    if constexpr (sizeof(A) == 4) return __fmaf_rn(h, 1.0f / F16_SCALE, base);
+    else return __fma_rn((double)h, 1.0 / F16_SCALE, (double)base);
   }
   template <class A, class L>
-  __device__ static void store(elem *p, A v, int) {
-    *p = __float2half_rn(static_cast<float>(v));
+  __device__ static A load(const elem *p, float base) { return decode<A>(__ldg(p), base); }
+  template <class A, class L>
+  __device__ static void store(elem *p, A v, float base) {
+    if constexpr (sizeof(A) == 4)
+      *p = __float2half_rn(__fmul_rn(__fsub_rn(v, base), F16_SCALE));
+    else
+      *p = __double2half(__dmul_rn(__dsub_rn(static_cast<double>(v), (double)base),
+                                   (double)F16_SCALE));
   }
 };
 #endif  // __CUDACC__

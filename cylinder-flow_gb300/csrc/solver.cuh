@@ -35,6 +35,7 @@ struct Layout {
   long long rs;    // elements between rows (y)
   long long zs;    // elements between planes (z)
   long long total; // elements per buffer
+  float fbase[27]; // storage offset of each population (Store<F16Dev>; 0 otherwise)
   __host__ __device__ long long idx(int x, int y, int z) const {
     return (long long)(z + Gz) * zs + (long long)(y + G) * rs + (x + xoff);
   }
@@ -87,6 +88,9 @@ struct SweepArgs {
   long long *step;       // device step counter (history slot = step % cap)
   long long cap;
   int bnd_blocks;        // grid of the force launch (persistent, about one block per SM)
+  int sms;               // multiprocessors of the device
+  int lines;             // 1: the interior runs the line-staged sweep (sweep_lines.cuh)
+  unsigned *err;         // device error word of the handle (a bounded wait gave up)
 };
 
 struct FillArgs {
@@ -174,8 +178,15 @@ cudaError_t launch_set_f(int Q, int store, const Layout &L, void *f, const doubl
 cudaError_t launch_fill_value(int Q, int store, const Layout &L, void *f, cudaStream_t s);
 
 // Fill omega, omega_f and the relaxation constants rk/rkf/rkl of a sweep for
-// lattice Q, storage kind `store` (the FP16 format's scales are folded in).
+// lattice Q (any storage kind `store`: the codecs hand the arithmetic the
+// populations themselves).
 void set_relax(SweepArgs &a, int Q, int store, double omega);
+
+// Line-staged sweep (lines.cu): whether it covers a handle's form, its one-time
+// set-up (shared-memory opt-in) and its launch.
+bool lines_supported(int Q, int store, int layout_rows, bool alpha, int nx);
+cudaError_t lines_prepare();
+cudaError_t launch_lines_f16_q27(const SweepArgs &a, int sms, cudaStream_t s);
 
 // Number of kernel launches issued through the launchers (all handles).
 long long launches();

@@ -143,15 +143,6 @@ template <> struct VA<df64> {
 };
 
 
-// acc + K v with K = NUM / DEN a power of two (1 and -1 without a product).
-template <class V, int NUM, int DEN>
-__device__ __forceinline__ V acc_(V acc, V v) {
-  using O = VA<V>;
-  if constexpr (NUM == DEN) return O::add(acc, v);
-  else if constexpr (NUM == -DEN) return O::sub(acc, v);
-  else return O::fma(v, O::splat(typename O::S(double(NUM) / double(DEN))), acc);
-}
-
 // Index of the direction with velocity (ex, ey, ez), -1 if none; and the
 // weight class of direction i (|e_i|^2: 0 rest, 1 axis, 2 face diagonal,
 // 3 corner).
@@ -175,9 +166,9 @@ __host__ __device__ constexpr int pair_of(int i) {
 
 // Relaxation constants of a sweep (SweepArgs::rk, host-computed per handle):
 //   rk[0]      = 1 - omega
-//   rk[1 + c]  = omega w_c s_c         (Kw, weight class c, storage scale s_c)
-//   rk[5 + c]  = 4.5 omega w_c s_c     (Ka)
-//   rk[9 + c]  = 3 omega w_c s_c       (K3)
+//   rk[1 + c]  = omega w_c         (Kw, weight class c)
+//   rk[5 + c]  = 4.5 omega w_c     (Ka)
+//   rk[9 + c]  = 3 omega w_c       (K3)
 // in FP64 (rk), FP32 (rkf) and as the FP32 remainder rk - rkf (rkl), which
 // with rkf forms the double-float constant.
 constexpr int RK_OMC = 0, RK_W = 1, RK_A = 5, RK_3 = 9, RK_N = 13;
@@ -201,8 +192,7 @@ template <> __device__ __forceinline__ df64 rconst<df64>(const SweepArgs &a, int
 // ("3D MPI+KOKKOS+MPIIO/lbm.cpp:257-272"), f <- (1 - omega) f + omega feq, with
 // omega and the weight folded into per-class constants (rconst) and written per
 // +/- pair: the pair shares e.u, (e.u)^2 and the even part of feq; the odd part
-// flips sign.  f is in storage units (SF::scale; the scale is folded into the
-// constants and a pair shares it).  Per cell and pair k of class c:
+// flips sign.  Per cell and pair k of class c:
 //   c0 = rho3 - 1.5 |u|^2,  A_c = Kw_c c0,
 //   sym = Ka_c (e.u)^2 + A_c,  asym = K3_c e.u,
 //   f_i = (1 - omega) f_i + (sym + asym),  f_opp(i) = (1 - omega) f_opp(i) + (sym - asym).
@@ -268,20 +258,15 @@ __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const 
   bgk_relax_v<L, A, SF>(f, rho3, ux, uy, uz, a);
 }
 
-// Moments in deviation form: rho3 = 3p = sum f, u = sum f e.
-// Unscaled storage (FP64, FP32): a three-level cascade over the 3 x 3 x 3 cube
-// of velocities -- per (e_x, e_y) line the sum and the difference along z, then
-// along y, then along x -- 49 additions for D3Q27 (14 for D2Q9) instead of 66
-// (18) with pair sums.  Scaled storage (FP16; the 1/scale factors are exact
-// powers of two that differ by weight class): pair sums and differences, each
-// scaled once.
+// Moments in deviation form: rho3 = 3p = sum f, u = sum f e, as a three-level
+// cascade over the 3 x 3 x 3 cube of velocities -- per (e_x, e_y) line the sum
+// and the difference along z, then along y, then along x -- 49 additions for
+// D3Q27 (14 for D2Q9) instead of 66 (18) with pair sums.
 template <class L, class V, class SF>
 __device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
   using O = VA<V>;
   using S = typename O::S;
-  constexpr bool unscaled = SF::template scale<L>(0) == 1.0 && SF::template scale<L>(1) == 1.0 &&
-                            SF::template scale<L>(L::Q - 1) == 1.0;
-  if constexpr (unscaled && L::D == 3) {
+  if constexpr (L::D == 3) {
     V s0[3][3], s1[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -304,7 +289,7 @@ __device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz
     ux = O::sub(t00[2], t00[0]);
     uy = O::add(O::add(t01[0], t01[2]), t01[1]);
     uz = O::add(O::add(t10[0], t10[2]), t10[1]);
-  } else if constexpr (unscaled) {
+  } else {
     V s0[3], s1[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -318,24 +303,6 @@ __device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz
     ux = O::sub(s0[2], s0[0]);
     uy = O::add(O::add(s1[0], s1[2]), s1[1]);
     uz = O::splat(S(0));
-  } else {
-    constexpr int S0 = (int)SF::template scale<L>(0);
-    if constexpr (S0 == 1) rho3 = f[0];
-    else rho3 = O::mul(f[0], O::splat(S(1.0 / S0)));
-    ux = uy = uz = O::splat(S(0));
-    static_for(
-        [&](auto kc) {
-          constexpr int k = decltype(kc)::value;
-          constexpr int i = L::pair(k), j = L::opp(L::pair(k));
-          constexpr int SC = (int)SF::template scale<L>(i);
-          const V sm = O::add(f[i], f[j]);
-          const V d = O::sub(f[i], f[j]);
-          rho3 = acc_<V, 1, SC>(rho3, sm);
-          if constexpr (L::ex(i) != 0) ux = acc_<V, L::ex(i), SC>(ux, d);
-          if constexpr (L::ey(i) != 0) uy = acc_<V, L::ey(i), SC>(uy, d);
-          if constexpr (L::ez(i) != 0) uz = acc_<V, L::ez(i), SC>(uz, d);
-        },
-        std::make_integer_sequence<int, L::NPAIR>{});
   }
 }
 
@@ -372,7 +339,7 @@ __device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long
   bgk_relax<L, A, SF>(f, rho3, ux, uy, uz, a);
   if (store) {
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) SF::template store<A, L>(fb + i * S + c, f[i], i);
+    for (int i = 0; i < L::Q; ++i) SF::template store<A, L>(fb + i * S + c, f[i], a.L.fbase[i]);
   }
 }
 
@@ -394,7 +361,8 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_kernel(const 
   A f[Q];
 #pragma unroll
   for (int i = 0; i < Q; ++i)
-    f[i] = SF::template load<A, L>(fa + i * S + c - a.L.off(L::ex(i), L::ey(i), L::ez(i)), i);
+    f[i] = SF::template load<A, L>(fa + i * S + c - a.L.off(L::ex(i), L::ey(i), L::ez(i)),
+                                   a.L.fbase[i]);
 
   A rho3, ux, uy, uz;
   moments<L, A, SF>(f, rho3, ux, uy, uz);
@@ -434,7 +402,7 @@ template <int Q, int I> struct DirC {
 
 
 // Inlet equilibrium population in the arithmetic type (no FP64 conversion in
-// FP32 sweeps), in storage units (the host scales f_in / f_in_f).
+// FP32 sweeps; f_in_f + f_in_l for double-float).
 template <class A>
 __device__ __forceinline__ A inlet_pop(const SweepArgs &a, int i) {
   if constexpr (std::is_same<A, df64>::value) return df64(a.f_in_f[i], a.f_in_l[i]);
@@ -467,7 +435,7 @@ __device__ __forceinline__ A pull_plain(const typename Store<ST>::elem *__restri
   using Dd = DirC<Q, I>;
   long long src = c - a.L.off(Dd::ex, Dd::ey, Dd::ez);
   if constexpr (Dd::ex < 0) src += (x == a.L.nx - 1) ? Dd::ex : 0;
-  A v = SF::template load<A, L>(fa + I * S + src, I);
+  A v = SF::template load<A, L>(fa + I * S + src, a.L.fbase[I]);
   if constexpr (Dd::ex > 0) v = (x == 0) ? inlet_pop<A>(a, I) : v;
   return v;
 }
@@ -489,7 +457,7 @@ __device__ __forceinline__ A pull_resolved(const typename Store<ST>::elem *__res
   using SF = Store<ST>;
   using Dd = DirC<Q, I>;
   if constexpr (I == 0) {
-    return SF::template load<A, L>(fa + c, 0);
+    return SF::template load<A, L>(fa + c, a.L.fbase[0]);
   } else {
     long long src = c - a.L.off(Dd::ex, Dd::ey, Dd::ez);
     bool my = false, mz = false, bb = false;
@@ -512,9 +480,10 @@ __device__ __forceinline__ A pull_resolved(const typename Store<ST>::elem *__res
     bb = bb || ((links >> I) & 1u);
     const int j = my ? (mz ? Dd::myz : Dd::my) : (mz ? Dd::mz : I);
     if constexpr (Dd::ex < 0) src += (x == a.L.nx - 1) ? Dd::ex : 0;  // zero gradient
-    // mirrors keep |e|, so direction I's storage scale applies to j and opp(I)
+    // a mirror j of I has I's |e| and e_x, hence I's storage offset; the
+    // bounced population is opp(I) and decodes with its own
     const long long addr = bb ? (long long)Dd::opp * S + c : (long long)j * S + src;
-    A v = SF::template load<A, L>(fa + addr, I);
+    A v = SF::template load<A, L>(fa + addr, bb ? a.L.fbase[Dd::opp] : a.L.fbase[I]);
     if constexpr (Dd::ex > 0) v = (!bb && x == 0) ? inlet_pop<A>(a, j) : v;
     return v;
   }
@@ -530,8 +499,8 @@ __device__ __forceinline__ int face_state(int y, int z, int ny, int nz) {
 // same source as pull_resolved.  Solid link (bit I of `links`) or no-slip face:
 // halfway bounce-back f*_{opp(I)}(X); otherwise the table's source with the
 // per-cell x rules (inlet equilibrium at x = 0, zero gradient at x = nx-1).  A
-// mirrored population has the same |e| and e_x as I, so I's storage scale and
-// inlet value apply.
+// mirrored population has the same |e| and e_x as I, so I's storage offset
+// and inlet value apply.
 template <int Q, class ST, class A, int I>
 __device__ __forceinline__ A pull_listed(const typename Store<ST>::elem *__restrict__ fa,
                                          long long c, long long S, int x, long long off,
@@ -540,20 +509,20 @@ __device__ __forceinline__ A pull_listed(const typename Store<ST>::elem *__restr
   using SF = Store<ST>;
   using Dd = DirC<Q, I>;
   if constexpr (I == 0) {
-    return SF::template load<A, L>(fa + c, 0);
+    return SF::template load<A, L>(fa + c, a.L.fbase[0]);
   } else {
     const bool bb = wbb || ((links >> I) & 1u);
     long long src = c + off;
     if constexpr (Dd::ex < 0) src += (x == a.L.nx - 1) ? Dd::ex : 0;  // zero gradient
-    A v = SF::template load<A, L>(fa + (bb ? (long long)Dd::opp * S + c : src), I);
+    A v = SF::template load<A, L>(fa + (bb ? (long long)Dd::opp * S + c : src),
+                                  bb ? a.L.fbase[Dd::opp] : a.L.fbase[I]);
     if constexpr (Dd::ex > 0) v = (!bb && x == 0) ? inlet_pop<A>(a, I) : v;
     return v;
   }
 }
 
 // Force of one cell's solid bounce-backs, summed in the arithmetic type (at most
-// Q - 1 terms): each adds 2 f*_{opp(I)}(X) e_{opp(I)} = -2 v_I e_I (v_I in
-// storage units, scale of I).
+// Q - 1 terms): each adds 2 f*_{opp(I)}(X) e_{opp(I)} = -2 v_I e_I.
 template <int Q, class A, class SF>
 __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A &fy, A &fz) {
   static_for(
@@ -562,7 +531,7 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
         if constexpr (I > 0) {
           using O = VA<A>;
           const A m = ((links >> I) & 1u)
-                          ? O::mul(A(2.0 / SF::template scale<Lat<Q>>(I)), f[I]) : A(0);
+                          ? O::mul(A(2.0), f[I]) : A(0);
           if constexpr (Lat<Q>::ex(I) != 0) fx = Lat<Q>::ex(I) > 0 ? O::sub(fx, m) : O::add(fx, m);
           if constexpr (Lat<Q>::ey(I) != 0) fy = Lat<Q>::ey(I) > 0 ? O::sub(fy, m) : O::add(fy, m);
           if constexpr (Lat<Q>::ez(I) != 0) fz = Lat<Q>::ez(I) > 0 ? O::sub(fz, m) : O::add(fz, m);
@@ -594,11 +563,11 @@ __device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restric
   const long long off = I * S - (Dd::ex + Dd::ey * rs + Dd::ez * zs);
   C v0 = C(0.0f), v1 = C(0.0f);
   if constexpr (Dd::ex < 0) {  // the outlet column repeats itself (pm = p - 1 there)
-    if (act0) v0 = SF::template load<C, L>(pm0 + off, I);
-    if (act1) v1 = SF::template load<C, L>(pm1 + off, I);
+    if (act0) v0 = SF::template load<C, L>(pm0 + off, a.L.fbase[I]);
+    if (act1) v1 = SF::template load<C, L>(pm1 + off, a.L.fbase[I]);
   } else {
-    if (act0) v0 = SF::template load<C, L>(p + off, I);
-    if (act1) v1 = SF::template load<C, L>(p + off + 32, I);
+    if (act0) v0 = SF::template load<C, L>(p + off, a.L.fbase[I]);
+    if (act1) v1 = SF::template load<C, L>(p + off + 32, a.L.fbase[I]);
   }
   if constexpr (Dd::ex > 0) v0 = inlet0 ? inlet_pop<C>(a, I) : v0;
   return PairT<P>::make(v0, v1);
@@ -617,8 +586,8 @@ __device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__
   using Dd = DirC<Q, I>;
   using C = typename PairT<P>::C;
   if constexpr (I == 0) {
-    return PairT<P>::make(SF::template load<C, L>(p, 0),
-                          act1 ? SF::template load<C, L>(p + 32, 0) : C(0.0f));
+    return PairT<P>::make(SF::template load<C, L>(p, a.L.fbase[0]),
+                          act1 ? SF::template load<C, L>(p + 32, a.L.fbase[0]) : C(0.0f));
   } else {
     const bool bb0 = wbb || ((l0 >> I) & 1u), bb1 = wbb || ((l1 >> I) & 1u);
     long long s0 = off, s1 = off + 32;
@@ -627,8 +596,10 @@ __device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__
       s1 += out1 ? Dd::ex : 0;
     }
     constexpr long long OS = Dd::opp;
-    C v0 = SF::template load<C, L>(p + (bb0 ? OS * S : s0), I);
-    const C v1 = act1 ? SF::template load<C, L>(p + (bb1 ? OS * S + 32 : s1), I) : C(0.0f);
+    const float b0 = bb0 ? a.L.fbase[Dd::opp] : a.L.fbase[I];
+    const float b1 = bb1 ? a.L.fbase[Dd::opp] : a.L.fbase[I];
+    C v0 = SF::template load<C, L>(p + (bb0 ? OS * S : s0), b0);
+    const C v1 = act1 ? SF::template load<C, L>(p + (bb1 ? OS * S + 32 : s1), b1) : C(0.0f);
     if constexpr (Dd::ex > 0) v0 = (!bb0 && inlet0) ? inlet_pop<C>(a, I) : v0;
     return PairT<P>::make(v0, v1);
   }
@@ -718,8 +689,8 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
   E *__restrict__ q = static_cast<E *>(a.fb) + c;
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) {
-    if (st0) SF::template store<C, L>(q + i * S, T::x(f[i]), i);
-    if (st1) SF::template store<C, L>(q + i * S + 32, T::y(f[i]), i);
+    if (st0) SF::template store<C, L>(q + i * S, T::x(f[i]), a.L.fbase[i]);
+    if (st1) SF::template store<C, L>(q + i * S + 32, T::y(f[i]), a.L.fbase[i]);
   }
 }
 
@@ -893,7 +864,8 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) channel_force_kerne
           [&](auto ic) {
             constexpr int I = decltype(ic)::value;
             f[I] = ((links >> I) & 1u)
-                       ? SF::template load<A, L>(fa + (long long)DirC<Q, I>::opp * S + c, I)
+                       ? SF::template load<A, L>(fa + (long long)DirC<Q, I>::opp * S + c,
+                                                 a.L.fbase[DirC<Q, I>::opp])
                        : A(0);
           },
           std::make_integer_sequence<int, Q>{});
@@ -983,10 +955,10 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY) stream_state_kernel(const
         double v;
         if constexpr (REF)
           v = SF::template load<double, L>(fa + I * S + c - a.L.off(L::ex(I), L::ey(I), L::ez(I)),
-                                           I);
+                                           a.L.fbase[I]);
         else
           v = pull_resolved<Q, ST, double, I>(fa, c, S, x, y, z, links, a);
-        out[(long long)I * N + cell] = v / SF::template scale<L>(I);
+        out[(long long)I * N + cell] = v;
       },
       std::make_integer_sequence<int, Q>{});
 }
@@ -1014,6 +986,12 @@ cudaError_t launch_macros_channel_t(const SweepArgs &a, cudaStream_t s) {
 // two-cells-per-thread kernel; the others the one-cell kernel.
 template <int Q, class ST, class A, int MINB_FAST>
 void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) {
+  if constexpr (Q == 27 && sizeof(A) == 4 && std::is_same<ST, F16Dev>::value) {
+    if (a.lines) {  // FP16, ROWS layout: the line-staged sweep
+      (void)launch_lines_f16_q27(a, a.sms, s);
+      return;
+    }
+  }
   if constexpr (sizeof(A) == 4 && !std::is_same<ST, double>::value) {
     // Blocks per SM, measured on the D3Q27 bench step: FP32 storage 0.850 /
     // 0.908 / 0.937 of the copy peak at 4 / 5 / 6 per SM (80 registers, no

@@ -46,9 +46,12 @@ def test_batch_instances_match_standalone_channels(cuda, storage):
             f_ref, h_ref, u_ref = alone(cfg, steps)
             inst = b.instance(k)
             assert inst.info().steps_done == steps
-            assert rel_err(inst.get_f(), f_ref) < 1e-6, k
-            assert rel_err(inst.force_history(), h_ref) < 1e-5, k
-            assert rel_err(inst.macros()[0], u_ref) < 1e-6, k
+            # the same cell arithmetic in the same order: identical states; the
+            # force sums run over the batch's own blocks, so their FP64
+            # summation order (not the per-cell terms) differs
+            assert np.array_equal(inst.get_f(), f_ref), k
+            assert np.array_equal(inst.macros()[0], u_ref), k
+            assert rel_err(inst.force_history(), h_ref) < 1e-12, k
 
 
 def test_batch_graph_replay_equals_single_steps(cuda):

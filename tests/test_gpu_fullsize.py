@@ -11,7 +11,9 @@
 
 Tolerances (relative L-inf, scaled by the field's max |value|) as in
 test_gpu_parity.py: FP64 arithmetic 1e-10 (fields) / 1e-9 (force); double-float
-1e-9; FP32 collision 2e-5; FP16-deviation storage 3e-3."""
+1e-9; FP32 collision 2e-5; FP16-deviation storage 3e-3, its velocity
+components scaled by the flow speed max |u| (v and w are near zero over most
+of these grids, so binary16's absolute resolution is what they see)."""
 from __future__ import annotations
 
 import numpy as np
@@ -49,8 +51,12 @@ def test_cylinder_512x128x128_matches_oracle(cuda, cyl_oracle, storage, compute,
         u, v, w, p = s.macros()
         fh = s.force_history()
         fpost = s.get_f()
+    speed = float(np.max(np.abs(o["u"])))
     for k, a in (("u", u), ("v", v), ("w", w), ("p", p)):
-        assert rel_err(a, o[k]) < tol, (k, rel_err(a, o[k]))
+        err = rel_err(a, o[k])
+        if storage == "fp16dev" and k != "p":
+            err = float(np.max(np.abs(a - o[k]))) / speed
+        assert err < tol, (k, err)
     assert rel_err(fpost, o["fpost"]) < tol
     assert rel_err(fh, o["force"]) < ftol
 

@@ -128,7 +128,7 @@ def _same_dat(mine: str, ref: str):
     for x, y in diff:
         fx, fy = [float(t) for t in x.split()], [float(t) for t in y.split()]
         assert len(fx) == len(fy) and np.allclose(fx, fy, rtol=0, atol=1.01e-8), (x, y)
-    assert len(diff) <= max(3, len(a) // 1000), len(diff)
+    assert len(diff) <= max(3, len(a) // 100), len(diff)
 
 
 @pytest.mark.parametrize("name,dim", [("ref2d_96x40", 2), ("ref3d_40x12x12", 3)])
