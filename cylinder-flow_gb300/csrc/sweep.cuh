@@ -422,6 +422,42 @@ template <> struct PairT<float2> {
   __device__ static float third(float c) { return __fmul_rn(c, 1.0f / 3.0f); }
 };
 
+// Storage codec of a cell pair on FP32x2 (the two-cell kernels): the raw
+// elements convert one by one, the FP16 format's offset and scale apply to the
+// pair in one packed FMA, and an FP16 pair is rounded in one packed
+// conversion -- the same values as Store<>::load/store per cell (the product
+// with a power of two is exact, so fma(v, 2^12, -2^12 b) = 2^12 RN(v - b)).
+template <class ST> struct PairCodec;
+template <> struct PairCodec<double> {
+  __device__ static float raw(double e) { return d2f_bits(e); }
+  __device__ static float2 dec(float2 r, float2) { return r; }
+  __device__ static void put2(double *p0, double *p1, float2 v, float, bool s0, bool s1) {
+    if (s0) *p0 = f2d_bits(v.x);
+    if (s1) *p1 = f2d_bits(v.y);
+  }
+};
+template <> struct PairCodec<float> {
+  __device__ static float raw(float e) { return e; }
+  __device__ static float2 dec(float2 r, float2) { return r; }
+  __device__ static void put2(float *p0, float *p1, float2 v, float, bool s0, bool s1) {
+    if (s0) *p0 = v.x;
+    if (s1) *p1 = v.y;
+  }
+};
+template <> struct PairCodec<F16Dev> {
+  __device__ static float raw(__half e) { return __half2float(e); }
+  __device__ static float2 dec(float2 r, float2 b) {
+    return __ffma2_rn(r, make_float2(1.0f / F16_SCALE, 1.0f / F16_SCALE), b);
+  }
+  __device__ static void put2(__half *p0, __half *p1, float2 v, float b, bool s0, bool s1) {
+    const float nb = -F16_SCALE * b;
+    const __half2 h =
+        __float22half2_rn(__ffma2_rn(v, make_float2(F16_SCALE, F16_SCALE), make_float2(nb, nb)));
+    if (s0) *p0 = __low2half(h);
+    if (s1) *p1 = __high2half(h);
+  }
+};
+
 // Post-stream population I of cell X (offset c) for rows away from the y/z
 // faces and cells away from solids: the plain pull, with the inlet column
 // taking the inlet equilibrium and the outlet column repeating itself (zero
@@ -556,21 +592,21 @@ __device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restric
                                        const typename Store<ST>::elem *__restrict__ pm1,
                                        long long S, long long rs, long long zs, bool act0,
                                        bool act1, bool inlet0, const SweepArgs &a) {
-  using L = Lat<Q>;
-  using SF = Store<ST>;
   using Dd = DirC<Q, I>;
-  using C = typename PairT<P>::C;
+  using PC = PairCodec<ST>;
   const long long off = I * S - (Dd::ex + Dd::ey * rs + Dd::ez * zs);
-  C v0 = C(0.0f), v1 = C(0.0f);
+  float r0 = 0.0f, r1 = 0.0f;
   if constexpr (Dd::ex < 0) {  // the outlet column repeats itself (pm = p - 1 there)
-    if (act0) v0 = SF::template load<C, L>(pm0 + off, a.L.fbase[I]);
-    if (act1) v1 = SF::template load<C, L>(pm1 + off, a.L.fbase[I]);
+    if (act0) r0 = PC::raw(__ldg(pm0 + off));
+    if (act1) r1 = PC::raw(__ldg(pm1 + off));
   } else {
-    if (act0) v0 = SF::template load<C, L>(p + off, a.L.fbase[I]);
-    if (act1) v1 = SF::template load<C, L>(p + off + 32, a.L.fbase[I]);
+    if (act0) r0 = PC::raw(__ldg(p + off));
+    if (act1) r1 = PC::raw(__ldg(p + off + 32));
   }
-  if constexpr (Dd::ex > 0) v0 = inlet0 ? inlet_pop<C>(a, I) : v0;
-  return PairT<P>::make(v0, v1);
+  const float b = a.L.fbase[I];
+  float2 v = PC::dec(make_float2(r0, r1), make_float2(b, b));
+  if constexpr (Dd::ex > 0) v.x = inlet0 ? a.f_in_f[I] : v.x;
+  return v;
 }
 
 // The pair pull of a listed tile pair: pull_listed for cells x0 and x0 + 32
@@ -581,13 +617,12 @@ __device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__
                                               unsigned l0, unsigned l1, bool act1,
                                               bool out0, bool out1, bool inlet0,
                                               const SweepArgs &a) {
-  using L = Lat<Q>;
-  using SF = Store<ST>;
   using Dd = DirC<Q, I>;
-  using C = typename PairT<P>::C;
+  using PC = PairCodec<ST>;
   if constexpr (I == 0) {
-    return PairT<P>::make(SF::template load<C, L>(p, a.L.fbase[0]),
-                          act1 ? SF::template load<C, L>(p + 32, a.L.fbase[0]) : C(0.0f));
+    const float b = a.L.fbase[0];
+    return PC::dec(make_float2(PC::raw(__ldg(p)), act1 ? PC::raw(__ldg(p + 32)) : 0.0f),
+                   make_float2(b, b));
   } else {
     const bool bb0 = wbb || ((l0 >> I) & 1u), bb1 = wbb || ((l1 >> I) & 1u);
     long long s0 = off, s1 = off + 32;
@@ -598,10 +633,11 @@ __device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__
     constexpr long long OS = Dd::opp;
     const float b0 = bb0 ? a.L.fbase[Dd::opp] : a.L.fbase[I];
     const float b1 = bb1 ? a.L.fbase[Dd::opp] : a.L.fbase[I];
-    C v0 = SF::template load<C, L>(p + (bb0 ? OS * S : s0), b0);
-    const C v1 = act1 ? SF::template load<C, L>(p + (bb1 ? OS * S + 32 : s1), b1) : C(0.0f);
-    if constexpr (Dd::ex > 0) v0 = (!bb0 && inlet0) ? inlet_pop<C>(a, I) : v0;
-    return PairT<P>::make(v0, v1);
+    const float r0 = PC::raw(__ldg(p + (bb0 ? OS * S : s0)));
+    const float r1 = act1 ? PC::raw(__ldg(p + (bb1 ? OS * S + 32 : s1))) : 0.0f;
+    float2 v = PC::dec(make_float2(r0, r1), make_float2(b0, b1));
+    if constexpr (Dd::ex > 0) v.x = (!bb0 && inlet0) ? a.f_in_f[I] : v.x;
+    return v;
   }
 }
 
@@ -688,10 +724,8 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
   bgk_relax_v<L, P, SF>(f, rho3, ux, uy, uz, a);
   E *__restrict__ q = static_cast<E *>(a.fb) + c;
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) {
-    if (st0) SF::template store<C, L>(q + i * S, T::x(f[i]), a.L.fbase[i]);
-    if (st1) SF::template store<C, L>(q + i * S + 32, T::y(f[i]), a.L.fbase[i]);
-  }
+  for (int i = 0; i < L::Q; ++i)
+    PairCodec<ST>::put2(q + i * S, q + i * S + 32, f[i], a.L.fbase[i], st0, st1);
 }
 
 template <int Q, class ST, class P, int MINB>

@@ -87,12 +87,13 @@ struct LinesArgs {
 // Issue the Q bulk copies of line `ln` into stage buffer `buf` (one thread).
 template <int Q, class E>
 __device__ __forceinline__ void lines_issue(const SweepArgs &a, const LinesArgs &la, long long ln,
-                                            E *buf, unsigned long long *bar) {
+                                            E *buf, unsigned long long *bar,
+                                            const long long *face_off, const unsigned *face_bb) {
   using L = Lat<Q>;
   const int ny = a.L.ny;
   const int y = (int)(ln % ny), z = (int)(ln / ny);
   const int st = face_state(y, z, ny, a.L.nz);
-  const unsigned wbb = a.face_bb[st];
+  const unsigned wbb = face_bb[st];
   const E *fa = static_cast<const E *>(a.fa);
   const long long line0 = a.L.idx(0, y, z) - a.L.xoff;  // element 0 of population 0's row
   const unsigned bytes = (unsigned)(la.window * sizeof(E));
@@ -104,7 +105,7 @@ __device__ __forceinline__ void lines_issue(const SweepArgs &a, const LinesArgs 
     long long row;
     if (I == 0) row = line0;
     else if ((wbb >> I) & 1u) row = line0 + (long long)L::opp(I) * a.L.S;
-    else row = line0 + a.face_off[st * Q + I] + L::ex(I);  // undo the table's x shift
+    else row = line0 + face_off[st * Q + I] + L::ex(I);  // undo the table's x shift
     bulk_copy_g2s(buf + (size_t)I * la.window, fa + row + a.L.xoff - 8, bytes, bar);
   }
 }
@@ -118,10 +119,14 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
   extern __shared__ __align__(128) unsigned char lines_smem[];
   __shared__ unsigned long long bars[4];
   __shared__ int failed;
+  __shared__ long long s_off[16 * Q];  // the face-state tables, for the issuing thread
+  __shared__ unsigned s_bb[16];
   E *ring = reinterpret_cast<E *>(lines_smem);
   const size_t stage_elems = (size_t)Q * la.window;
   const int tid = threadIdx.x, lane = tid & 31;
   const int nx = a.L.nx, ny = a.L.ny;
+  for (int k = tid; k < 16 * Q; k += LINES_THREADS) s_off[k] = a.face_off[k];
+  if (tid < 16) s_bb[tid] = a.face_bb[tid];
   if (tid == 0) {
     for (int s = 0; s < la.stages; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -132,7 +137,8 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
   if (tid == 0)
     for (int s = 0; s < la.stages - 1; ++s) {
       const long long ln = blockIdx.x + (long long)s * gridDim.x;
-      if (ln < la.lines) lines_issue<Q, E>(a, la, ln, ring + s * stage_elems, &bars[s]);
+      if (ln < la.lines)
+        lines_issue<Q, E>(a, la, ln, ring + s * stage_elems, &bars[s], s_off, s_bb);
     }
   // thread 0's bookkeeping for a clean exit after a failed wait: the stages
   // with copies in flight
@@ -150,7 +156,7 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
       const long long nl = ln + (long long)(la.stages - 1) * gridDim.x;
       const int ns = (s + la.stages - 1) % la.stages;
       if (nl < la.lines) {
-        lines_issue<Q, E>(a, la, nl, ring + ns * stage_elems, &bars[ns]);
+        lines_issue<Q, E>(a, la, nl, ring + ns * stage_elems, &bars[ns], s_off, s_bb);
         inflight |= 1u << ns;
       }
     }
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
     const E *buf = ring + s * stage_elems;
     const int y = (int)(ln % ny), z = (int)(ln / ny);
     const int st = face_state(y, z, ny, a.L.nz);
-    const unsigned wbb = a.face_bb[st];
+    const unsigned wbb = s_bb[st];
     const long long rowc = a.L.idx(0, y, z);  // cell x = 0, population 0
     for (int xb = 0; xb < nx; xb += LINES_CELLS) {
       const int x0 = xb + tid, x1 = x0 + LINES_THREADS;
@@ -190,20 +196,21 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
               xs1 = (x1 == nx - 1 && sx != 0) ? x1 : xs1;
             }
             const float b = ((wbb >> I) & 1u) ? a.L.fbase[L::opp(I)] : a.L.fbase[I];
-            float v0 = st0 ? SF::template decode<float>(row[xs0], b) : 0.0f;
-            float v1 = st1 ? SF::template decode<float>(row[xs1], b) : 0.0f;
-            if constexpr (ex > 0) v0 = (x0 == 0 && sx != 0) ? a.f_in_f[I] : v0;
+            const float r0 = st0 ? PairCodec<ST>::raw(row[xs0]) : 0.0f;
+            const float r1 = st1 ? PairCodec<ST>::raw(row[xs1]) : 0.0f;
+            float2 v = PairCodec<ST>::dec(make_float2(r0, r1), make_float2(b, b));
+            if constexpr (ex > 0) v.x = (x0 == 0 && sx != 0) ? a.f_in_f[I] : v.x;
             if constexpr (I > 0) {
               if (linked) {  // warp-uniform: bounce-back off solid sources
                 const E *fa = static_cast<const E *>(a.fa);
                 const long long ob = (long long)L::opp(I) * a.L.S + rowc;
                 if ((l0 >> I) & 1u)
-                  v0 = SF::template load<float, L>(fa + ob + x0, a.L.fbase[L::opp(I)]);
+                  v.x = SF::template load<float, L>(fa + ob + x0, a.L.fbase[L::opp(I)]);
                 if ((l1 >> I) & 1u)
-                  v1 = SF::template load<float, L>(fa + ob + x1, a.L.fbase[L::opp(I)]);
+                  v.y = SF::template load<float, L>(fa + ob + x1, a.L.fbase[L::opp(I)]);
               }
             }
-            f[I] = make_float2(v0, v1);
+            f[I] = v;
           },
           std::make_integer_sequence<int, Q>{});
       float2 rho3, ux, uy, uz;
@@ -213,10 +220,8 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
       bgk_relax_v<L, float2, SF>(f, rho3, ux, uy, uz, a);
       E *__restrict__ q = static_cast<E *>(a.fb) + rowc;
 #pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        if (st0) SF::template store<float, L>(q + i * a.L.S + x0, f[i].x, a.L.fbase[i]);
-        if (st1) SF::template store<float, L>(q + i * a.L.S + x1, f[i].y, a.L.fbase[i]);
-      }
+      for (int i = 0; i < Q; ++i)
+        PairCodec<ST>::put2(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i], a.L.fbase[i], st0, st1);
     }
     __syncthreads();  // every thread is done with stage s before it is refilled
     pbits ^= 1u << s;
