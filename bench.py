@@ -365,8 +365,9 @@ def run_channel2d(args):
     forms = {}
     n_launch = 0
     with ClockSampler(local) as clk:
-        for name, st, cp in (("fp64", "fp64", "fp64"), ("fp64_store", "fp64", "fp32"),
-                             ("fp32_store", "fp32", "fp32"), ("fp16dev_store", "fp16dev", "fp32")):
+        for name, st, cp in (("fp64", "fp64", "fp64"), ("df64", "fp64", "df64"),
+                             ("fp64_store", "fp64", "fp32"), ("fp32_store", "fp32", "fp32"),
+                             ("fp16dev_store", "fp16dev", "fp32")):
             with cflbm.Solver(device=local, storage=st, compute=cp, force_history=steps + 8,
                               **CH2D) as s:
                 stream = torch.cuda.ExternalStream(s.stream_ptr())
@@ -394,11 +395,15 @@ def run_channel2d(args):
             forms[name] = {"mlups": round(world * CH2D_CELLS * steps / (ms * 1e-3) / 1e6, 2),
                            "us_per_step": round(1e3 * ms / steps, 3),
                            "bytes_per_cell": info.bytes_per_cell_step,
-                           "cd_mean": stats["cd_mean"], "cl_rms": stats["cl_rms"],
+                           "cd_mean": stats["cd_mean"],
+                           "cd_mean_periods": stats["cd_mean_periods"],
+                           "periods": stats["periods"], "cl_rms": stats["cl_rms"],
                            "st": stats["st"]}
     ref = forms["fp64"]
     for v in forms.values():
         v["cd_rel_err"] = abs(v["cd_mean"] - ref["cd_mean"]) / abs(ref["cd_mean"])
+        v["cd_periods_rel_err"] = (abs(v["cd_mean_periods"] - ref["cd_mean_periods"])
+                                   / abs(ref["cd_mean_periods"]))
         v["st_rel_err"] = abs(v["st"] - ref["st"]) / abs(ref["st"]) if ref["st"] else None
 
     # ---- end to end, plain FP64 form: solid mask from the host, the run, the

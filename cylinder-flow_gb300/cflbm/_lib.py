@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(_HERE, "libcflbm.so")
 D2Q9, D3Q27 = 9, 27
 STORE_FP64, STORE_FP32, STORE_FP16DEV = 0, 1, 2
 COMPUTE_FP64, COMPUTE_FP32, COMPUTE_DF64 = 0, 1, 2
-PROFILE_CHANNEL, PROFILE_REF2D, PROFILE_REF3D = 0, 1, 2
+PROFILE_CHANNEL, PROFILE_REF2D, PROFILE_REF3D, PROFILE_REF2DS = 0, 1, 2, 3
 WALL_FREESLIP, WALL_NOSLIP, WALL_PERIODIC = 0, 1, 2
 GEOM_NONE, GEOM_CYLINDER, GEOM_SPHERE = 0, 1, 2
 LAYOUT_SOA, LAYOUT_ROWS = 0, 1

@@ -20,13 +20,14 @@ class Solver:
     shape) and ``ref_ran`` (int32 over the reference's ghosted box) are numpy
     arrays.  ``storage``/``compute``/``profile``/``wall_*``/``geom`` accept the
     integer constants or the names "fp64", "fp32", "fp16dev", "channel",
-    "ref2d", "ref3d", "freeslip", "noslip", "periodic", "cylinder", "sphere".
+    "ref2d", "ref3d", "ref2ds", "freeslip", "noslip", "periodic", "cylinder", "sphere".
     """
 
     _names = {
         "storage": {"fp64": C.STORE_FP64, "fp32": C.STORE_FP32, "fp16dev": C.STORE_FP16DEV},
         "compute": {"fp64": C.COMPUTE_FP64, "fp32": C.COMPUTE_FP32, "df64": C.COMPUTE_DF64},
         "profile": {"channel": C.PROFILE_CHANNEL, "ref2d": C.PROFILE_REF2D,
+                    "ref2ds": C.PROFILE_REF2DS,
                     "ref3d": C.PROFILE_REF3D},
         "wall_y": {"freeslip": C.WALL_FREESLIP, "noslip": C.WALL_NOSLIP,
                    "periodic": C.WALL_PERIODIC},

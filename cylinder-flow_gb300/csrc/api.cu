@@ -327,10 +327,11 @@ int validate(const cflbm_config *c) {
     return fail(CFLBM_E_INVALID, "compute %d unknown", c->compute);
   if (c->compute == CFLBM_COMPUTE_DF64 && c->storage != CFLBM_STORE_FP64)
     return fail(CFLBM_E_INVALID, "double-float arithmetic needs FP64 storage");
-  if (c->profile < 0 || c->profile > 2)
+  if (c->profile < 0 || c->profile > 3)
     return fail(CFLBM_E_INVALID, "profile %d unknown", c->profile);
-  if (c->profile == CFLBM_PROFILE_REF2D && c->lattice != CFLBM_D2Q9)
-    return fail(CFLBM_E_INVALID, "REF2D profile needs the D2Q9 lattice");
+  if ((c->profile == CFLBM_PROFILE_REF2D || c->profile == CFLBM_PROFILE_REF2DS) &&
+      c->lattice != CFLBM_D2Q9)
+    return fail(CFLBM_E_INVALID, "REF2D/REF2DS profiles need the D2Q9 lattice");
   if (c->profile == CFLBM_PROFILE_REF3D && c->lattice != CFLBM_D3Q27)
     return fail(CFLBM_E_INVALID, "REF3D profile needs the D3Q27 lattice");
   if (c->wall_y < 0 || c->wall_y > 2 || c->wall_z < 0 || c->wall_z > 2)
@@ -407,7 +408,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   // the last ghost (the reference's wall pass reads two cells beyond the ring).
   const int es = store_size(cfg->storage);
   h->esize = es;
-  const int G = cfg->profile == CFLBM_PROFILE_CHANNEL ? 1 : (cfg->profile == CFLBM_PROFILE_REF2D ? 2 : 3);
+  const int G = cfg->profile == CFLBM_PROFILE_CHANNEL ? 1 : (cfg->profile == CFLBM_PROFILE_REF3D ? 3 : 2);
   const int align = 128 / es;
   Layout &L = h->L;
   L.nx = nx;
@@ -446,6 +447,10 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   RefSetup ref;
   if (cfg->profile == CFLBM_PROFILE_REF2D) {
     ref2d_setup(nx, ny, cfg->u0, cfg->ref_ran, ref);
+    solid = ref.solid;
+    h->area = ref.area;
+  } else if (cfg->profile == CFLBM_PROFILE_REF2DS) {
+    ref2ds_setup(nx, ny, cfg->u0, cfg->ref_ran, ref);
     solid = ref.solid;
     h->area = ref.area;
   } else if (cfg->profile == CFLBM_PROFILE_REF3D) {
@@ -737,11 +742,14 @@ static int one_step(cflbm_handle *h, bool write_macros) {
     h->macros_pending = true;
     return CFLBM_OK;
   }
-  if (h->cfg.profile == CFLBM_PROFILE_REF2D) {
+  if (h->cfg.profile == CFLBM_PROFILE_REF2D || h->cfg.profile == CFLBM_PROFILE_REF2DS) {
     // "MPI Kokkos/lbm.cpp:315-345": inlet, outlet, then the two wall rows.
     // Each pair (the two ends of one axis) writes and reads disjoint layers, so a
-    // pair runs as one launch; the pairs keep the reference's order.
-    const FaceOp ops[4] = {{0, 0, 0}, {1, 0, 1}, {2, 1, 0}, {2, 1, 1}};
+    // pair runs as one launch; the pairs keep the reference's order.  The serial
+    // variant's wall rows ("Kokkos/lbm.cpp:158-168") leave out the two corner
+    // nodes of each ghost row.
+    const int trim = h->cfg.profile == CFLBM_PROFILE_REF2DS ? 1 : 0;
+    const FaceOp ops[4] = {{0, 0, 0, 0}, {1, 0, 1, 0}, {2, 1, 0, trim}, {2, 1, 1, trim}};
     for (int k = 0; k < 4; k += 2)
       CK_CUDA(launch_face_ops(Q, st, fa, ops[k], ops[k + 1], h->stream));
   } else {

@@ -198,6 +198,8 @@ __global__ void face_op_kernel(const FillArgs a, const FaceOp op0, const FaceOp 
   const int pa = blockIdx.x * blockDim.x + threadIdx.x - 1;
   const int pb = blockIdx.y + b0;
   if (pa >= na - 1) return;
+  const int trim = second ? op1.trim : op0.trim;
+  if (trim && (pa < 0 || pa >= na - 2)) return;  // the ghost ends of the range
   const int ex = DT<Q>::ex(i), ey = DT<Q>::ey(i), ez = DT<Q>::ez(i);
   const int ea = ax == 0 ? ex : (ax == 1 ? ey : ez);
   const int eta = ax == 0 ? ey : ex;                        // e along tangential a

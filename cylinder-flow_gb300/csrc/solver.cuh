@@ -19,7 +19,7 @@
 
 namespace cflbm {
 
-enum Profile { PROFILE_CHANNEL = 0, PROFILE_REF2D = 1, PROFILE_REF3D = 2 };
+enum Profile { PROFILE_CHANNEL = 0, PROFILE_REF2D = 1, PROFILE_REF3D = 2, PROFILE_REF2DS = 3 };
 enum Wall { WALL_FREESLIP = 0, WALL_NOSLIP = 1, WALL_PERIODIC = 2 };
 enum StoreKind { STORE_F64 = 0, STORE_F32 = 1, STORE_F16 = 2 };
 enum ComputeKind { COMPUTE_F64 = 0, COMPUTE_F32 = 1, COMPUTE_DF64 = 2 };
@@ -107,6 +107,7 @@ struct FaceOp {
   int kind;  // 0 copy (inlet), 1 extrapolate (outlet), 2 bounce (wall)
   int axis;  // 0 x, 1 y, 2 z
   int side;  // 0 low, 1 high
+  int trim;  // 1: the pass skips the two ghost ends of its tangential range
   int ndir;  // the populations the pass writes (filled by launch_face_ops),
   unsigned long long dirs;  // 5 bits each, the k-th at bit 5k
 };

@@ -23,9 +23,11 @@
 // FP32x2, two cells per thread: x and x + 256), so the states are bit-identical
 // to the register-fed kernel's.
 //
-// Every wait on an mbarrier is bounded; a wait that gives up records
-// LINES_TIMEOUT in *a.err (read by the host at the next synchronising call),
-// waits (bounded) for the copies the block has in flight, and returns.
+// One thread of the block waits for a stage's copies (bounded) and the block
+// meets it at one barrier per line, which also orders the reads of the stage
+// before its refill.  A wait that gives up records LINES_TIMEOUT in *a.err
+// (read by the host at the next synchronising call), waits (bounded) for the
+// copies the block has in flight, and returns.
 #pragma once
 #include "sweep.cuh"
 
@@ -147,11 +149,21 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
     for (int k = 0; k < la.stages - 1; ++k)
       if (blockIdx.x + (long long)k * gridDim.x < la.lines) inflight |= 1u << k;
   int s = 0;
-  unsigned pbits = 0u;  // bit k: parity of the next wait on stage k
-  for (long long ln = blockIdx.x; ln < la.lines; ln += gridDim.x) {
-    // refill the stage freed by the previous iteration with the line
-    // stages - 1 ahead (the __syncthreads at the end of the last iteration
-    // ordered every read of that stage before this)
+  unsigned pbits = 0u;  // bit k: parity of the next wait on stage k (thread 0)
+  // One thread waits for a stage's copies; the block meets it at one barrier
+  // per line, so no other warp spends issue slots polling the mbarrier.
+  if (tid == 0 && blockIdx.x < la.lines) {
+    if (mbar_wait_bounded(&bars[0], 0u)) {
+      inflight &= ~1u;
+      pbits ^= 1u;
+    } else {
+      failed = 1;
+    }
+  }
+  __syncthreads();
+  for (long long ln = blockIdx.x; ln < la.lines && !failed; ln += gridDim.x) {
+    // refill the stage the previous line used with the line stages - 1 ahead
+    // (every thread passed the barrier after finishing that line)
     if (tid == 0) {
       const long long nl = ln + (long long)(la.stages - 1) * gridDim.x;
       const int ns = (s + la.stages - 1) % la.stages;
@@ -160,13 +172,6 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
         inflight |= 1u << ns;
       }
     }
-    if (!mbar_wait_bounded(&bars[s], (pbits >> s) & 1u)) {
-      failed = 1;  // benign race: every writer writes 1
-    } else if (tid == 0) {
-      inflight &= ~(1u << s);
-    }
-    __syncthreads();
-    if (failed) break;
     const E *buf = ring + s * stage_elems;
     const int y = (int)(ln % ny), z = (int)(ln / ny);
     const int st = face_state(y, z, ny, a.L.nz);
@@ -223,9 +228,19 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
       for (int i = 0; i < Q; ++i)
         PairCodec<ST>::put2(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i], a.L.fbase[i], st0, st1);
     }
-    __syncthreads();  // every thread is done with stage s before it is refilled
-    pbits ^= 1u << s;
-    s = s + 1 == la.stages ? 0 : s + 1;
+    // the next line's stage: thread 0 waits for its copies, then the barrier
+    // (which also orders every read of stage s before its refill)
+    const int s1 = s + 1 == la.stages ? 0 : s + 1;
+    if (tid == 0 && ln + gridDim.x < la.lines) {
+      if (mbar_wait_bounded(&bars[s1], (pbits >> s1) & 1u)) {
+        inflight &= ~(1u << s1);
+        pbits ^= 1u << s1;
+      } else {
+        failed = 1;
+      }
+    }
+    __syncthreads();
+    s = s1;
   }
   if (failed && tid == 0) {
     atomicExch(la.err, LINES_TIMEOUT);

@@ -63,7 +63,8 @@ void System::read(const std::string &path) {
       if (error.empty()) error = "input.in: cflbm." + key + " has no value";
     } else if (key == "profile")
       pick(key, v, {{"channel", CFLBM_PROFILE_CHANNEL}, {"ref2d", CFLBM_PROFILE_REF2D},
-                    {"ref3d", CFLBM_PROFILE_REF3D}}, profile);
+                    {"ref3d", CFLBM_PROFILE_REF3D}, {"ref2ds", CFLBM_PROFILE_REF2DS}},
+           profile);
     else if (key == "storage")
       pick(key, v, {{"fp64", CFLBM_STORE_FP64}, {"fp32", CFLBM_STORE_FP32},
                     {"fp16dev", CFLBM_STORE_FP16DEV}}, storage);

@@ -90,6 +90,31 @@ LBM::LBM(MPI_Comm comm_, int sx, int sy, double &tau, double &rho0_, double &u0_
   apply_input_extensions(config);
 }
 
+LBM::LBM(int sx, int sy, double &tau, double &rho0_, double &u0_)
+    : glx(sx + 1), gly(sy + 1), glz(1), rho0(rho0_), tau0(tau), u0(u0_), dim(2), serial(true),
+      ua(this, 0), va(this, 1), wa(this, 2), p(this, 3), f(this), usr(this), rho(this) {
+  const int G = ghost_of(2);
+  l_l[0] = glx;
+  l_l[1] = gly;
+  l_l[2] = 1;
+  for (int d = 0; d < 3; ++d) {
+    l_s[d] = G;
+    l_e[d] = G + l_l[d];
+  }
+  lx = sx + 5;
+  ly = sy + 5;
+  lz = 1;
+  x_hi = glx - 1;
+  y_hi = gly - 1;
+  cflbm_config_default(&config);
+  config.lattice = CFLBM_D2Q9;
+  config.profile = CFLBM_PROFILE_REF2DS;
+  config.nx = glx;
+  config.ny = gly;
+  config.nz = 1;
+  apply_input_extensions(config);
+}
+
 LBM::~LBM() {
   if (h_) {
     try {
@@ -169,7 +194,7 @@ const std::vector<uint8_t> &LBM::solid() {
 // to test.dat.  Kept on the GPU and appended in bulk here.
 void LBM::flush_forces() {
   flush_steps();
-  if (dim != 2 || !h_) return;
+  if (dim != 2 || serial || !h_) return;  // the serial variant writes no test.dat
   cflbm_info info;
   check(cflbm_get_info(h_, &info), "cflbm_get_info");
   const int64_t todo = info.steps_done - forces_flushed_;
@@ -197,10 +222,24 @@ void LBM::MPIoutput(int n) {
 void LBM::Output(int n) {
   flush_forces();
   std::ofstream out;
-  const std::string name = "output" + std::to_string(n) + std::to_string(comm.me) + ".dat";
+  // The serial variant names its files output<n>.dat and writes x as
+  // 4 (i - 2) / (lx - 5) ("Kokkos/lbm.cpp:219-243").
+  const std::string name =
+      "output" + std::to_string(n) + (serial ? "" : std::to_string(comm.me)) + ".dat";
   out << std::setiosflags(std::ios::fixed);
   out.open(name, std::ios::out);
-  if (dim == 2) {
+  if (dim == 2 && serial) {
+    const auto &u = field(0), &v = field(1), &pp = field(3);
+    out << "variables=x,y,u,v,p" << std::endl;
+    out << "zone I=" << lx - 4 << ",J=" << ly - 4 << std::endl;
+    for (int j = 0; j < gly; ++j)
+      for (int i = 0; i < glx; ++i) {
+        const size_t c = (size_t)j * glx + i;
+        out << std::setprecision(8) << std::setiosflags(std::ios::left)
+            << 4 * (double)i / (lx - 5.0) << " " << (double)j / (ly - 5.0) << " " << u[c] << " "
+            << v[c] << " " << pp[c] << std::endl;
+      }
+  } else if (dim == 2) {
     const auto &u = field(0), &v = field(1), &pp = field(3);
     out << "variables=x,y,u,v,p" << std::endl;
     out << "zone I=" << lx - 4 << ",J=" << ly - 4 << std::endl;

@@ -5,6 +5,8 @@
 //        LBM(MPI_Comm, int sx, int sy, int sz, double &tau, double &rho0, double &u0)
 //   2-D: "MPI Kokkos/lbm.hpp:64-128"
 //        LBM(MPI_Comm, int sx, int sy, double &tau, double &rho0, double &u0)
+//   2-D serial: "Kokkos/lbm.hpp:20-70"
+//        LBM(int sx, int sy, double &tau, double &rho0, double &u0)
 // so the reference's main() drives it unchanged.  All state lives on the GPU
 // behind the C ABI (include/cflbm.h); the rank count is one, so
 // setup_subdomain/pack/exchange/unpack do nothing.  Collision() accounts for one
@@ -101,6 +103,7 @@ struct LBM {
   int x_lo = 0, x_hi = 0, y_lo = 0, y_hi = 0, z_lo = 0, z_hi = 0;
   double rho0, mu = 0, cs2 = 1.0 / 3.0, tau0, u0;
   int dim;
+  bool serial = false;  // the serial 2-D variant (its Output file name and coordinates)
   HostField ua, va, wa, p;
   HostPops f;
   HostUsr usr;
@@ -108,6 +111,9 @@ struct LBM {
 
   LBM(MPI_Comm comm_, int sx, int sy, int sz, double &tau, double &rho0_, double &u0_);
   LBM(MPI_Comm comm_, int sx, int sy, double &tau, double &rho0_, double &u0_);
+  // The serial 2-D variant ("Kokkos/lbm.hpp:26"): LBM(sx, sy, tau, rho0, u0) with
+  // lx = sx + 5, ly = sy + 5, i.e. (sx + 1) x (sy + 1) interior nodes.
+  LBM(int sx, int sy, double &tau, double &rho0_, double &u0_);
   ~LBM();
   LBM(const LBM &) = delete;
   LBM &operator=(const LBM &) = delete;

@@ -50,8 +50,18 @@ enum cflbm_compute { CFLBM_COMPUTE_FP64 = 0, CFLBM_COMPUTE_FP32 = 1, CFLBM_COMPU
  *           (Poiseuille inlet override, p = 0 outlet, its wall and solid rules,
  *           disk of diameter 0.03125*(nx-1) at the box centre).
  *  REF3D:   the reference's 3-D solver at one rank, "3D MPI+KOKKOS+MPIIO/lbm.cpp"
- *           (sphere at ((nx-1)/8)^3, radius (nx-1)/64). */
-enum cflbm_profile { CFLBM_PROFILE_CHANNEL = 0, CFLBM_PROFILE_REF2D = 1, CFLBM_PROFILE_REF3D = 2 };
+ *           (sphere at ((nx-1)/8)^3, radius (nx-1)/64).
+ *  REF2DS:  the reference's serial 2-D solver, "Kokkos/lbm.cpp" (its LBM(sx, sy)
+ *           is nx = sx + 1 by ny = sy + 1 interior nodes; disk at
+ *           (0.25 (nx - 1), 0.5 (ny + 3)) of its ghosted box with radius
+ *           0.1 (ny - 1); Poiseuille u times (1 + 0.001 ran); wall ghost rows
+ *           without their corner nodes; no force in the reference). */
+enum cflbm_profile {
+  CFLBM_PROFILE_CHANNEL = 0,
+  CFLBM_PROFILE_REF2D = 1,
+  CFLBM_PROFILE_REF3D = 2,
+  CFLBM_PROFILE_REF2DS = 3
+};
 enum cflbm_wall { CFLBM_WALL_FREESLIP = 0, CFLBM_WALL_NOSLIP = 1, CFLBM_WALL_PERIODIC = 2 };
 enum cflbm_geom { CFLBM_GEOM_NONE = 0, CFLBM_GEOM_CYLINDER = 1, CFLBM_GEOM_SPHERE = 2 };
 /* Population layout in device memory (x fastest in both):

@@ -4,7 +4,8 @@
   restatement of the reference) into oracle/liboracle.so.
 * ``build_ref()`` compiles the reference's own, unmodified sources from
   ``/root/reference`` against the Kokkos/MPI subset shim in oracle/shim/ into
-  oracle/_ref/ref2d and oracle/_ref/ref3d (drivers: oracle/ref_driver_*.cpp).
+  oracle/_ref/ref2d, oracle/_ref/ref3d and oracle/_ref/ref2ds (the serial
+  "Kokkos/" variant) (drivers: oracle/ref_driver_*.cpp).
   It needs the reference checkout and is skipped where that is absent.
 
 Both use the same flags (-O3, no fast-math, -ffp-contract=off), so the
@@ -48,8 +49,8 @@ def build_oracle(force: bool = False) -> str:
 
 
 def reference_available() -> bool:
-    return os.path.isdir(os.path.join(REFERENCE, "MPI Kokkos")) and os.path.isdir(
-        os.path.join(REFERENCE, "3D MPI+KOKKOS+MPIIO"))
+    return all(os.path.isdir(os.path.join(REFERENCE, d))
+               for d in ("MPI Kokkos", "3D MPI+KOKKOS+MPIIO", "Kokkos"))
 
 
 def build_ref(force: bool = False) -> list[str]:
@@ -72,9 +73,14 @@ def build_ref(force: bool = False) -> list[str]:
     out3 = os.path.join(outdir, "ref3d")
     if force or _stale(out3, src3 + shim_hdrs):
         jobs.append(["g++", *CXXFLAGS, "-w", "-I", shim, "-I", d3, *src3, "-o", out3])
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    d2s = os.path.join(REFERENCE, "Kokkos")
+    src2s = [os.path.join(HERE, "ref_driver_2ds.cpp"), os.path.join(d2s, "lbm.cpp")]
+    out2s = os.path.join(outdir, "ref2ds")
+    if force or _stale(out2s, src2s + shim_hdrs):
+        jobs.append(["g++", *CXXFLAGS, "-w", "-I", shim, "-I", d2s, *src2s, "-o", out2s])
+    with ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(_run, jobs))
-    return [out2, out3]
+    return [out2, out3, out2s]
 
 
 if __name__ == "__main__":

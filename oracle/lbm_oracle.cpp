@@ -272,6 +272,142 @@ int oracle_ref2d_run(int nx, int ny, double tau0, double u0, const int *ran, int
 }
 
 // ---------------------------------------------------------------------------
+// Reference profile, 2-D serial: "Kokkos/lbm.cpp" (one process; its LBM(sx, sy)
+// builds lx = sx + 5, ly = sy + 5, lbm.hpp:26, so the interior is nx = sx + 1 by
+// ny = sy + 1 nodes with two ghost layers on each side, lx = nx + 4).
+//
+// ran      : lx*ly ints, the reference's per-node draw (index i*ly+j).
+// f_out    : 9*lx*ly post-stream populations after `steps` steps (or null).
+// fpost_out: the same after one further Collision() (or null).
+// u/v/p_out: lx*ly macroscopic fields after `steps` steps (or null).
+// The variant computes no force.
+// ---------------------------------------------------------------------------
+int oracle_ref2ds_run(int nx, int ny, double tau0, double u0, const int *ran, int steps,
+                      double *f_out, double *fpost_out, double *u_out, double *v_out,
+                      double *p_out, int nthreads) {
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  const Lattice &L = lat2();
+  const int Q = 9;
+  const int lx = nx + 4, ly = ny + 4;
+  const long N = (long)lx * ly;
+  std::vector<double> f(Q * N, 0.0), ft(Q * N, 0.0), ua(N, 0.0), va(N, 0.0), p(N, 0.0);
+  std::vector<int> usr(N, 0);
+  auto F = [&](int ii, int i, int j) -> double & { return f[((long)ii * lx + i) * ly + j]; };
+  auto FT = [&](int ii, int i, int j) -> double & { return ft[((long)ii * lx + i) * ly + j]; };
+  auto A = [&](std::vector<double> &a, int i, int j) -> double & { return a[(long)i * ly + j]; };
+  auto U = [&](int i, int j) -> int & { return usr[(long)i * ly + j]; };
+  const auto &e = L.e;
+  const auto &t = L.t;
+  const auto &bb = L.bb;
+
+  // Initialize: "Kokkos/lbm.cpp:105-133": a disk at (0.25 (lx - 5), 0.5 (ly - 1))
+  // in box coordinates with r^2 = 0.01 (ly - 5)^2, Poiseuille u times
+  // (1 + 0.001 ran), f = feq.
+#pragma omp parallel for collapse(2)
+  for (int i = 0; i < lx; ++i)
+    for (int j = 0; j < ly; ++j) {
+      A(p, i, j) = 0.0;
+      U(i, j) = 1;
+      if (std::pow((i - 0.25 * (lx - 5)), 2) + std::pow((j - 0.5 * (ly - 1)), 2) <=
+          0.01 * (ly - 5) * (ly - 5))
+        U(i, j) = 0;
+      A(ua, i, j) = (u0 * 4.0 * (j - 2) * (ly - 3 - j) / std::pow((ly - 5), 2)) * U(i, j) *
+                    (1.0 + ran[(long)i * ly + j] * 0.001);
+      A(va, i, j) = 0.0;
+    }
+#pragma omp parallel for collapse(2)
+  for (int ii = 0; ii < Q; ++ii)
+    for (int i = 0; i < lx; ++i)
+      for (int j = 0; j < ly; ++j) {
+        F(ii, i, j) = t[ii] * A(p, i, j) * 3.0 +
+                      t[ii] * (3.0 * (e[ii][0] * A(ua, i, j) + e[ii][1] * A(va, i, j)) +
+                               4.5 * std::pow(e[ii][0] * A(ua, i, j) + e[ii][1] * A(va, i, j), 2) -
+                               1.5 * (std::pow(A(ua, i, j), 2) + std::pow(A(va, i, j), 2)));
+      }
+
+  auto collision = [&]() {
+    // "Kokkos/lbm.cpp:134-144".
+#pragma omp parallel for collapse(2)
+    for (int ii = 0; ii < Q; ++ii)
+      for (int i = 2; i < lx - 2; ++i)
+        for (int j = 2; j < ly - 2; ++j) {
+          double feq = t[ii] * A(p, i, j) * 3.0 +
+                       t[ii] * (3.0 * (e[ii][0] * A(ua, i, j) + e[ii][1] * A(va, i, j)) +
+                                4.5 * std::pow(e[ii][0] * A(ua, i, j) + e[ii][1] * A(va, i, j), 2) -
+                                1.5 * (std::pow(A(ua, i, j), 2) + std::pow(A(va, i, j), 2)));
+          F(ii, i, j) -= (F(ii, i, j) - feq) / (tau0 + 0.5);
+        }
+  };
+
+  for (int it = 1; it <= steps; ++it) {
+    collision();
+    // Streaming, "Kokkos/lbm.cpp:145-186".  Inlet copy and outlet extrapolation
+    // over j in [1, ly - 1) (:147-156).
+    for (int j = 1; j < ly - 1; ++j) {
+      F(1, 1, j) = F(1, 2, j);
+      F(5, 1, j) = F(5, 2, j);
+      F(8, 1, j) = F(8, 2, j);
+      F(3, lx - 2, j) = F(3, lx - 3, j);
+      F(7, lx - 2, j) = F(7, lx - 3, j - 1);
+      F(6, lx - 2, j) = F(6, lx - 3, j + 1);
+    }
+    // Wall rows over i in [2, lx - 2) only (:158-168): the corners i = 1 and
+    // i = lx - 2 of the ghost rows keep what the inlet/outlet pass left.
+    for (int i = 2; i < lx - 2; ++i) {
+      F(2, i, 1) = F(4, i, 3);
+      F(5, i, 1) = F(7, i + 2, 3);
+      F(6, i, 1) = F(8, i - 2, 3);
+      F(4, i, ly - 2) = F(2, i, ly - 4);
+      F(7, i, ly - 2) = F(5, i - 2, ly - 4);
+      F(8, i, ly - 2) = F(6, i + 2, ly - 4);
+    }
+    // Solid nodes next to fluid, over the whole box (:170-176).
+    for (int ii = 0; ii < Q; ++ii)
+      for (int i = 0; i < lx; ++i)
+        for (int j = 0; j < ly; ++j)
+          if (U(i, j) == 0 && U(i + e[ii][0], j + e[ii][1]) == 1)
+            F(ii, i, j) = F(bb[ii], i + 2 * e[ii][0], j + 2 * e[ii][1]);
+    // Pull stream into ft over [1, lx - 1) x [1, ly - 1), copy back over the
+    // interior (:177-186).
+#pragma omp parallel for collapse(2)
+    for (int ii = 0; ii < Q; ++ii)
+      for (int i = 1; i < lx - 1; ++i)
+        for (int j = 1; j < ly - 1; ++j) FT(ii, i, j) = F(ii, i - e[ii][0], j - e[ii][1]);
+#pragma omp parallel for collapse(2)
+    for (int ii = 0; ii < Q; ++ii)
+      for (int i = 2; i < lx - 2; ++i)
+        for (int j = 2; j < ly - 2; ++j) F(ii, i, j) = FT(ii, i, j);
+    // Update, serial host loop ("Kokkos/lbm.cpp:188-217"), j outer.
+    std::fill(ua.begin(), ua.end(), 0.0);
+    std::fill(va.begin(), va.end(), 0.0);
+    std::fill(p.begin(), p.end(), 0.0);
+    for (int j = 2; j < ly - 2; ++j)
+      for (int i = 2; i < lx - 2; ++i) {
+        for (int ii = 0; ii < Q; ++ii) {
+          A(p, i, j) = A(p, i, j) + F(ii, i, j) / 3.0;
+          A(ua, i, j) = A(ua, i, j) + F(ii, i, j) * e[ii][0];
+          A(va, i, j) = A(va, i, j) + F(ii, i, j) * e[ii][1];
+        }
+        A(ua, i, j) = A(ua, i, j) * U(i, j);
+        A(va, i, j) = A(va, i, j) * U(i, j);
+        A(p, i, j) = A(p, i, j) * U(i, j);
+        A(ua, 2, j) = u0 * 4.0 * (j - 2) * (ly - 3 - j) / std::pow((ly - 5), 2);
+        A(va, 2, j) = 0.0;
+        A(p, lx - 3, j) = 0.0;
+      }
+  }
+  if (f_out) std::memcpy(f_out, f.data(), sizeof(double) * Q * N);
+  if (u_out) std::memcpy(u_out, ua.data(), sizeof(double) * N);
+  if (v_out) std::memcpy(v_out, va.data(), sizeof(double) * N);
+  if (p_out) std::memcpy(p_out, p.data(), sizeof(double) * N);
+  if (fpost_out) {
+    collision();
+    std::memcpy(fpost_out, f.data(), sizeof(double) * Q * N);
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Reference profile, 3-D: "3D MPI+KOKKOS+MPIIO/lbm.cpp" at one rank
 // (ghost = 3, lx = nx + 6 ..., l_s = 3, l_e = 3 + n; lbm.hpp:146-219).
 // Arguments as oracle_ref2d_run, arrays over lx*ly*lz (index (i*ly+j)*lz+k).

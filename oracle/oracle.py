@@ -45,6 +45,9 @@ def lib():
         L.oracle_ref2d_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double, _ip, ctypes.c_int, _dp, _dp, _dp,
                                        _dp, _dp, _dp, ctypes.c_int]
+        L.oracle_ref2ds_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, _ip, ctypes.c_int, _dp, _dp, _dp,
+                                        _dp, _dp, ctypes.c_int]
         L.oracle_ref3d_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_double, ctypes.c_double, _ip, ctypes.c_int,
                                        _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]
@@ -82,6 +85,20 @@ def ref2d(nx, ny, tau0, u0, ran, steps, nthreads=0):
                                 _p(out["force"]), nthreads)
     assert rc == 0
     out["force"] = out["force"][:steps]
+    return out
+
+
+def ref2ds(nx, ny, tau0, u0, ran, steps, nthreads=0):
+    """Run the serial 2-D reference restatement ("Kokkos/lbm.cpp"); nx, ny are the
+    interior nodes (the reference's sx + 1, sy + 1); arrays keep its ghost ring."""
+    lx, ly = nx + 4, ny + 4
+    ran = np.ascontiguousarray(ran, np.int32).reshape(lx, ly)
+    out = dict(f=np.zeros((9, lx, ly)), fpost=np.zeros((9, lx, ly)), u=np.zeros((lx, ly)),
+               v=np.zeros((lx, ly)), p=np.zeros((lx, ly)))
+    rc = lib().oracle_ref2ds_run(nx, ny, tau0, u0, _p(ran, _ip), steps, _p(out["f"]),
+                                 _p(out["fpost"]), _p(out["u"]), _p(out["v"]), _p(out["p"]),
+                                 nthreads)
+    assert rc == 0
     return out
 
 
@@ -167,6 +184,23 @@ def run_ref2d_binary(nx, ny, tau0, u0, steps, outdir=None):
     subprocess.run([exe, outdir, str(nx), str(ny), repr(tau0), repr(u0), str(steps)],
                    check=True, capture_output=True)
     lx, ly = nx + 4, ny + 4
+    rd = lambda n, dt=np.float64: np.fromfile(os.path.join(outdir, n), dt)  # noqa: E731
+    return dict(dir=outdir, ran=rd("ran.i32", np.int32).reshape(lx, ly),
+                f=rd("f.f64").reshape(9, lx, ly), fpost=rd("fpost.f64").reshape(9, lx, ly),
+                u=rd("u.f64").reshape(lx, ly), v=rd("v.f64").reshape(lx, ly),
+                p=rd("p.f64").reshape(lx, ly))
+
+
+def run_ref2ds_binary(sx, sy, tau0, u0, steps, outdir=None):
+    """The compiled serial 2-D reference ("Kokkos/"); its interior is (sx + 1) x
+    (sy + 1) nodes."""
+    exe = ref_binary("ref2ds")
+    if exe is None:
+        return None
+    outdir = outdir or tempfile.mkdtemp(prefix="ref2ds_")
+    subprocess.run([exe, outdir, str(sx), str(sy), repr(tau0), repr(u0), str(steps)],
+                   check=True, capture_output=True)
+    lx, ly = sx + 5, sy + 5
     rd = lambda n, dt=np.float64: np.fromfile(os.path.join(outdir, n), dt)  # noqa: E731
     return dict(dir=outdir, ran=rd("ran.i32", np.int32).reshape(lx, ly),
                 f=rd("f.f64").reshape(9, lx, ly), fpost=rd("fpost.f64").reshape(9, lx, ly),

@@ -1,8 +1,9 @@
 """The small benchmark problem at full length on the GPU: D2Q9 400x100 cylinder
 channel, 20,000 steps, against the oracle's fixture (tests/golden/
-make_channel_golden.py).  Early forces are compared step by step; Cd mean, Cl
-rms and St over the last 10,000 steps are compared as statistics, since vortex
-shedding amplifies round-off differences in the phase."""
+make_channel_golden.py).  Early forces are compared step by step; the drag
+averaged over the whole shedding periods of the last 10,000 steps, the lift rms
+and St are compared as statistics, since vortex shedding amplifies round-off
+differences in the phase."""
 from __future__ import annotations
 
 import json
@@ -25,11 +26,15 @@ def fixture():
     return meta, z["force"], z["u"], z["v"]
 
 
+# tol_stats bounds the relative error of the drag averaged over whole shedding
+# periods (analysis.summary's cd_mean_periods) and of St; the lift rms gets 5x.
+# FP16 deviation storage is held to the 1e-3 drag bar of the precision form.
 @pytest.mark.parametrize("storage,compute,tol_f,tol_stats", [
-    ("fp64", "fp64", 1e-9, 2e-3),
-    ("fp64", "fp32", 1e-4, 1e-2),
-    ("fp32", "fp32", 1e-4, 1e-2),
-    ("fp16dev", "fp32", 5e-2, 5e-2),
+    ("fp64", "fp64", 1e-9, 1e-3),
+    ("fp64", "df64", 1e-9, 1e-3),
+    ("fp64", "fp32", 1e-4, 1e-3),
+    ("fp32", "fp32", 1e-4, 1e-3),
+    ("fp16dev", "fp32", 5e-2, 1e-3),
 ])
 def test_config1_statistics_match_oracle(cuda, storage, compute, tol_f, tol_stats):
     meta, force, _, _ = fixture()
@@ -42,6 +47,8 @@ def test_config1_statistics_match_oracle(cuda, storage, compute, tol_f, tol_stat
     assert np.max(np.abs(hist[:k, 0] - force[:k, 0])) <= tol_f * scale
     st = analysis.summary(hist, case["u0"], case["diam"], case["diam"], meta["window"])
     ref = meta["stats"]
-    assert abs(st["cd_mean"] - ref["cd_mean"]) <= tol_stats * abs(ref["cd_mean"])
+    assert st["periods"] >= 3 and ref["periods"] >= 3
+    assert abs(st["cd_mean_periods"] - ref["cd_mean_periods"]) <= tol_stats * abs(
+        ref["cd_mean_periods"])
     assert abs(st["cl_rms"] - ref["cl_rms"]) <= 5 * tol_stats * abs(ref["cl_rms"])
     assert abs(st["st"] - ref["st"]) <= tol_stats * abs(ref["st"])

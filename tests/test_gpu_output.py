@@ -77,13 +77,15 @@ int main(int argc, char **argv) {
   const int dim = std::atoi(argv[1]), nx = std::atoi(argv[2]), ny = std::atoi(argv[3]),
             nz = std::atoi(argv[4]), steps = std::atoi(argv[7]);
   double tau = std::atof(argv[5]), u0 = std::atof(argv[6]), rho0 = 1.0;
-  const int G = dim == 2 ? 2 : 3;
-  std::vector<int32_t> ran((size_t)(nx + 2 * G) * (ny + 2 * G) * (dim == 2 ? 1 : nz + 2 * G));
+  const int G = dim <= 2 ? 2 : 3;
+  std::vector<int32_t> ran((size_t)(nx + 2 * G) * (ny + 2 * G) * (dim <= 2 ? 1 : nz + 2 * G));
   std::FILE *fp = std::fopen(argv[8], "rb");
   if (!fp || std::fread(ran.data(), 4, ran.size(), fp) != ran.size()) return 3;
   std::fclose(fp);
-  LBM *l = dim == 2 ? new LBM(MPI_COMM_WORLD, nx, ny, tau, rho0, u0)
-                    : new LBM(MPI_COMM_WORLD, nx, ny, nz, tau, rho0, u0);
+  // dim 1: the serial 2-D variant, LBM(sx, sy) with sx = nx - 1, sy = ny - 1
+  LBM *l = dim == 1 ? new LBM(nx - 1, ny - 1, tau, rho0, u0)
+           : dim == 2 ? new LBM(MPI_COMM_WORLD, nx, ny, tau, rho0, u0)
+                      : new LBM(MPI_COMM_WORLD, nx, ny, nz, tau, rho0, u0);
   l->config.ref_ran = ran.data();
   l->Initialize();
   l->Output(0);
@@ -94,9 +96,11 @@ int main(int argc, char **argv) {
   }
   l->Output(1);
   // the f, usr and rho views at an interior node next to the body's centre
-  std::printf("%.17g %d %.17g\n", dim == 2 ? l->f(1, G + 1, G + 1) : l->f(1, G + 1, G + 1, G + 1),
-              dim == 2 ? l->usr(G + nx / 2, G + ny / 2) : l->usr(G + 1, G + 1, G + 1),
-              dim == 2 ? l->rho(G, G) : l->rho(G, G, G));
+  std::printf("%.17g %d %.17g\n", dim <= 2 ? l->f(1, G + 1, G + 1) : l->f(1, G + 1, G + 1, G + 1),
+              dim == 1   ? l->usr((int)(0.25 * (nx - 1) + 0.5), (ny + 3) / 2)  // disk centre
+              : dim == 2 ? l->usr(G + nx / 2, G + ny / 2)                     // disk centre
+                         : l->usr(G + 1, G + 1, G + 1),
+              dim <= 2 ? l->rho(G, G) : l->rho(G, G, G));
   delete l;
   return 0;
 }
@@ -131,7 +135,8 @@ def _same_dat(mine: str, ref: str):
     assert len(diff) <= max(3, len(a) // 100), len(diff)
 
 
-@pytest.mark.parametrize("name,dim", [("ref2d_96x40", 2), ("ref3d_40x12x12", 3)])
+@pytest.mark.parametrize("name,dim", [("ref2d_96x40", 2), ("ref3d_40x12x12", 3),
+                                      ("ref2ds_96x36", 1)])
 def test_dropin_output_files_match_reference(cuda, output_exe, tmp_path, name, dim):
     g = load_golden(name)
     m = g["meta"]
@@ -142,12 +147,15 @@ def test_dropin_output_files_match_reference(cuda, output_exe, tmp_path, name, d
                        cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     for k in (0, 1):
-        _same_dat(str(tmp_path / f"output{k}0.dat"), os.path.join(GOLDEN, f"{name}_output{k}0.dat"))
+        if dim == 1:  # the serial variant's files are output<n>.dat
+            _same_dat(str(tmp_path / f"output{k}.dat"), os.path.join(GOLDEN, f"{name}_output{k}.dat"))
+        else:
+            _same_dat(str(tmp_path / f"output{k}0.dat"),
+                      os.path.join(GOLDEN, f"{name}_output{k}0.dat"))
     f1, usr, rho = r.stdout.split()[-3:]
-    G = 2 if dim == 2 else 3
-    if dim == 2:
+    if dim <= 2:
         assert float(f1) == pytest.approx(g["fstream"][1, 1, 1], rel=1e-11, abs=1e-15)
-        assert usr == "0"  # the disk's centre
+        assert usr == "0"  # at the disk's centre
     else:
         assert float(f1) == pytest.approx(g["fstream"][1, 1, 1, 1], rel=1e-11, abs=1e-15)
         assert usr == "1"

@@ -64,6 +64,39 @@ def test_ref3d_matches_reference_golden(cuda):
         assert rel_err(r[k], g[k]) < TOL64, k
 
 
+def test_ref2ds_matches_reference_golden(cuda):
+    """The serial "Kokkos/" variant (its own geometry, perturbation and wall
+    rows without corners) against the compiled reference's outputs."""
+    g = load_golden("ref2ds_96x36")
+    m = g["meta"]
+    with Solver(lattice=9, nx=m["nx"], ny=m["ny"], profile="ref2ds", tau0=m["tau0"],
+                u0=m["u0"], ref_ran=g["ran"]) as s:
+        s.step(m["steps"])
+        u, v, w, p = s.macros()
+        fstream = s.get_f_stream()[:, 0]
+        fpost = s.get_f()[:, 0]
+    assert rel_err(u[0], g["u"]) < TOL64
+    assert rel_err(v[0], g["v"]) < TOL64
+    assert rel_err(p[0], g["p"]) < TOL64
+    assert rel_err(fpost, g["fpost"]) < TOL64
+    assert rel_err(fstream, g["fstream"]) < TOL64
+
+
+@pytest.mark.parametrize("compute,tol", [("fp64", 1e-10), ("df64", 1e-9), ("fp32", 2e-5)])
+def test_ref2ds_matches_oracle_longer_run(cuda, compute, tol):
+    nx, ny, steps = 240, 64, 800
+    ran = np.random.default_rng(11).integers(0, 100, size=(nx + 4, ny + 4)).astype(np.int32)
+    o = O.ref2ds(nx, ny, 0.03, 0.06, ran, steps)
+    with Solver(lattice=9, nx=nx, ny=ny, profile="ref2ds", tau0=0.03, u0=0.06, ref_ran=ran,
+                compute=compute) as s:
+        s.step(steps)
+        u, v, w, p = s.macros()
+    sl = (slice(2, 2 + nx), slice(2, 2 + ny))
+    assert rel_err(u[0], o["u"][sl].T) < tol
+    assert rel_err(v[0], o["v"][sl].T) < tol
+    assert rel_err(p[0], o["p"][sl].T) < tol
+
+
 def test_ref2d_matches_oracle_longer_run(cuda):
     nx, ny, steps = 256, 72, 600
     ran = np.random.default_rng(7).integers(0, 100, size=(nx + 4, ny + 4)).astype(np.int32)

@@ -42,6 +42,29 @@ def test_ref2d_matches_reference_golden():
     assert np.max(np.abs(cl - g["cdcl"][:, 1])) <= 6e-17 * max(1.0, np.max(np.abs(cl)))
 
 
+def test_ref2ds_matches_reference_golden():
+    """The serial "Kokkos/" variant: restatement against the compiled
+    reference's own outputs, bit for bit."""
+    g = load_golden("ref2ds_96x36")
+    m = g["meta"]
+    o = O.ref2ds(m["nx"], m["ny"], m["tau0"], m["u0"], g["ran"], m["steps"])
+    G = 2
+    sl = (slice(G, G + m["nx"]), slice(G, G + m["ny"]))
+    assert np.array_equal(o["fpost"][(slice(None),) + sl].transpose(0, 2, 1), g["fpost"])
+    assert np.array_equal(o["f"][(slice(None),) + sl].transpose(0, 2, 1), g["fstream"])
+    for k in ("u", "v", "p"):
+        assert np.array_equal(o[k][sl].T, g[k]), k
+
+
+@pytest.mark.skipif(not obuild.reference_available(), reason="reference checkout absent")
+def test_ref2ds_oracle_matches_compiled_reference_other_size():
+    obuild.build_ref()
+    r = O.run_ref2ds_binary(127, 47, 0.02, 0.08, 120)
+    o = O.ref2ds(128, 48, 0.02, 0.08, r["ran"], 120)
+    for k in ("f", "fpost", "u", "v", "p"):
+        assert np.array_equal(o[k], r[k]), k
+
+
 def test_ref3d_matches_reference_golden():
     g = load_golden("ref3d_40x12x12")
     m = g["meta"]
