@@ -44,38 +44,40 @@ def strouhal(cl: np.ndarray, diam: float, u0: float, dt: float = 1.0) -> float:
     return float(freq * diam / u0)
 
 
-def shedding_periods(cl: np.ndarray) -> tuple[int, int, int]:
-    """(first, last, periods): the steps of the first and last upward zero
-    crossing of the lift about its mean, which bound a whole number of shedding
-    periods, and that number; (0, n, 0) when the lift crosses fewer than twice.
-    """
-    x = np.asarray(cl, np.float64)
-    x = x - np.mean(x)
-    up = np.nonzero((x[:-1] < 0.0) & (x[1:] >= 0.0))[0] + 1
-    if up.size < 2:
-        return 0, x.size, 0
-    return int(up[0]), int(up[-1]), int(up.size - 1)
+def shedding_window(cl: np.ndarray, diam: float, u0: float) -> tuple[int, int]:
+    """(start, periods): the last whole shedding periods of a lift series -- the
+    period from the Strouhal number (the periodogram peak, robust to noise on
+    the lift), the largest whole number of periods that fits, counted back from
+    the series' end.  (0, 0) when the lift does not oscillate."""
+    st = strouhal(cl, diam, u0)
+    n = np.asarray(cl).size
+    if not np.isfinite(st) or st <= 0.0:
+        return 0, 0
+    period = diam / (st * u0)  # steps
+    k = int(n // period)
+    if k < 1:
+        return 0, 0
+    return n - int(round(k * period)), k
 
 
 def summary(force: np.ndarray, u0: float, area: float, diam: float, window: int | None = None):
     """Mean Cd, rms Cl and St over the last `window` steps.
 
     cd_mean is the plain window mean.  cd_mean_periods averages the drag over
-    the whole shedding periods inside the window (between the first and the
-    last upward zero crossing of the lift): in periodic shedding the drag
-    oscillates at twice the shedding frequency, and a window that ends mid-cycle
-    moves the plain mean by a part of that oscillation's amplitude -- so two
-    runs whose shedding phases differ by a fraction of a period differ in
-    cd_mean without differing in mean drag.  Equal to cd_mean when the lift
-    does not oscillate."""
+    the last whole shedding periods inside the window (shedding_window): in
+    periodic shedding the drag oscillates at twice the shedding frequency, and a
+    window that ends mid-cycle moves the plain mean by a part of that
+    oscillation's amplitude -- so two runs whose shedding phases differ by a
+    fraction of a period differ in cd_mean without differing in mean drag.
+    Equal to cd_mean when the lift does not oscillate."""
     cc = coefficients(force, u0, area)
     if window:
         cc = cc[-window:]
     cd, cl = cc[:, 0], cc[:, 1]
-    a, b, n = shedding_periods(cl)
+    a, n = shedding_window(cl, diam, u0)
     return {
         "cd_mean": float(np.mean(cd)),
-        "cd_mean_periods": float(np.mean(cd[a:b])) if n else float(np.mean(cd)),
+        "cd_mean_periods": float(np.mean(cd[a:])) if n else float(np.mean(cd)),
         "periods": n,
         "cl_rms": float(np.sqrt(np.mean((cl - np.mean(cl)) ** 2))),
         "st": strouhal(cl, diam, u0),

@@ -9,6 +9,7 @@
 #include <thread>
 #include <vector>
 #include "handle.hpp"
+#include "setup.cuh"
 
 using namespace cflbm;
 
@@ -128,70 +129,6 @@ void build_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
   }
 }
 
-// Channel-profile solid links: bit i of cell X is set when the source of
-// population i, X - e_i mapped onto the box exactly as the sweep maps it
-// (periodic wrap / free-slip mirror / no-slip wall / inlet / zero-gradient
-// outlet), is a solid cell -- i.e. when the sweep must bounce population i back.
-// Every source lies within one cell of X in each axis, so only cells within one
-// cell (in x) of a solid of a neighbouring row can have bits: each row scans the
-// x-range spanned by the solids of its (up to 3 x 3) source rows.
-template <int Q>
-std::vector<uint32_t> channel_links(const std::vector<uint8_t> &solid, int nx, int ny, int nz,
-                                    int wall_y, int wall_z) {
-  using L = Lat<Q>;
-  std::vector<uint32_t> bits(solid.size(), 0u);
-  const long long rows = (long long)ny * nz;
-  std::vector<int> rmin(rows, nx), rmax(rows, -1);
-  host_parallel_rows(rows, [&](long long r) {
-    const uint8_t *row = &solid[(size_t)r * nx];
-    for (int x = 0; x < nx; ++x)
-      if (row[x]) {
-        rmin[r] = std::min(rmin[r], x);
-        rmax[r] = x;
-      }
-  });
-  host_parallel_rows(rows, [&](long long r) {
-    const int y = (int)(r % ny), z = (int)(r / ny);
-    int lo = nx, hi = -1;
-    for (int dz = (Q == 27 ? -1 : 0); dz <= (Q == 27 ? 1 : 0); ++dz)
-      for (int dy = -1; dy <= 1; ++dy) {
-        int zz = z + dz, yy = y + dy;
-        if (zz < 0 || zz >= nz) {
-          if (wall_z != CFLBM_WALL_PERIODIC) continue;
-          zz = (zz + nz) % nz;
-        }
-        if (yy < 0 || yy >= ny) {
-          if (wall_y != CFLBM_WALL_PERIODIC) continue;
-          yy = (yy + ny) % ny;
-        }
-        const long long q = (long long)zz * ny + yy;
-        lo = std::min(lo, rmin[q]);
-        hi = std::max(hi, rmax[q]);
-      }
-    for (int x = std::max(0, lo - 1); x <= std::min(nx - 1, hi + 1); ++x) {
-      uint32_t b = 0u;
-      for (int i = 1; i < Q; ++i) {
-        int sx = x - L::ex(i), sy = y - L::ey(i), sz = z - L::ez(i);
-        if (Q == 27 && (sz < 0 || sz >= nz)) {
-          if (wall_z == CFLBM_WALL_PERIODIC) sz = (sz + nz) % nz;
-          else if (wall_z == CFLBM_WALL_FREESLIP) sz = z;
-          else continue;  // no-slip wall, not the body
-        }
-        if (sy < 0 || sy >= ny) {
-          if (wall_y == CFLBM_WALL_PERIODIC) sy = (sy + ny) % ny;
-          else if (wall_y == CFLBM_WALL_FREESLIP) sy = y;
-          else continue;
-        }
-        if (sx < 0) continue;  // inlet
-        if (sx >= nx) sx = nx - 1;
-        if (solid[((size_t)sz * ny + sy) * nx + sx]) b |= 1u << i;
-      }
-      bits[((size_t)z * ny + y) * nx + x] = b;
-    }
-  });
-  return bits;
-}
-
 // Pull tables of the listed tiles, one row per face state (bit 0: y = 0, bit 1:
 // y = ny-1, bit 2: z = 0, bit 3: z = nz-1).  For every direction i: the source
 // offset relative to the cell, population slot included, after the sweep's y/z
@@ -227,50 +164,6 @@ void face_tables(const Layout &Ly, int wall_y, int wall_z, std::vector<long long
       off[(size_t)st * Q + i] = (long long)j * Ly.S + src;
       if (b) bb[st] |= 1u << i;
     }
-}
-
-// Warp tiles (32 cells of one row; tile = (z*ny + y)*nxw + x/32) on a y/z face
-// row or holding a solid cell or a cell with solid links: the sweep pulls them
-// through the face-state tables and their link words, and the force launch
-// walks their list.  Fills the list and the 32 link words of every listed tile
-// (bit 31: solid cell); returns the per-tile flags.
-std::vector<unsigned char> solid_tiles(const std::vector<uint8_t> &solid,
-                                       const std::vector<uint32_t> &bits, int nx, int ny,
-                                       int nz, int nxw, std::vector<int> &list,
-                                       std::vector<uint32_t> &tile_bits) {
-  std::vector<unsigned char> flag((size_t)nxw * ny * nz, 0);
-  // Rows in parallel, concatenated in row order (the list is ordered by tile).
-  const long long rows = (long long)ny * nz;
-  std::vector<std::vector<int>> per(rows);
-  host_parallel_rows(rows, [&](long long r) {
-    const int y = (int)(r % ny), z = (int)(r / ny);
-    for (int w = 0; w < nxw; ++w) {
-      // Rows on a y or z face always need the resolving pull.
-      bool any = y == 0 || y == ny - 1 || (nz > 1 && (z == 0 || z == nz - 1));
-      for (int x = w * 32; x < std::min(nx, (w + 1) * 32) && !any; ++x) {
-        const size_t n = (size_t)r * nx + x;
-        any = solid[n] || bits[n];
-      }
-      if (!any) continue;
-      const size_t t = (size_t)r * nxw + w;
-      flag[t] = 1;
-      per[r].push_back((int)t);
-    }
-  });
-  list.clear();
-  for (long long r = 0; r < rows; ++r) list.insert(list.end(), per[r].begin(), per[r].end());
-  tile_bits.assign(list.size() * 32, 0u);
-  host_parallel_rows((long long)list.size(), [&](long long k) {
-    const long long t = list[k];
-    const long long r = t / nxw;
-    const int w = (int)(t % nxw);
-    for (int l = 0; l < 32; ++l) {
-      const int x = w * 32 + l;
-      tile_bits[(size_t)k * 32 + l] =
-          x < nx ? bits[(size_t)r * nx + x] | (solid[(size_t)r * nx + x] ? 1u << 31 : 0u) : 0u;
-    }
-  });
-  return flag;
 }
 
 // Equilibrium of the channel inlet (p = 0, u = (u_in, 0, 0)) in storage format
@@ -458,14 +351,18 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     solid = ref.solid;
     h->area = ref.area;
   } else {
-    channel_mask(*cfg, solid);  // cfg->solid (nonzero = solid) when given, else the geometry
+    // channel: the mask, links and listed tiles are built on the GPU below
     h->area = channel_area(h->cfg);
   }
+  const bool chan = cfg->profile == CFLBM_PROFILE_CHANNEL;
   std::vector<int4> links;
-  if (d3) build_links<27>(solid, nx, ny, nz, links, h->n_solid);
-  else build_links<9>(solid, nx, ny, nz, links, h->n_solid);
-  h->n_links = (long long)links.size();
-  const std::vector<uint32_t> mask = pack_mask(solid, nx, ny, nz, h->nxw);
+  std::vector<uint32_t> mask;
+  if (!chan) {
+    if (d3) build_links<27>(solid, nx, ny, nz, links, h->n_solid);
+    else build_links<9>(solid, nx, ny, nz, links, h->n_solid);
+    h->n_links = (long long)links.size();
+    mask = pack_mask(solid, nx, ny, nz, h->nxw);
+  }
 
   // Device allocations.
   const size_t N = (size_t)nx * ny * nz;
@@ -476,8 +373,10 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   h->buf[1] = h->fB;
   CK_CUDA(cudaMemsetAsync(h->fA, 0, h->f_bytes, h->stream));
   CK_CUDA(cudaMemsetAsync(h->fB, 0, h->f_bytes, h->stream));
-  if ((rc = dev_alloc_t(h, &h->d_mask, mask.size()))) return rc;
-  CK_CUDA(cudaMemcpyAsync(h->d_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if ((rc = dev_alloc_t(h, &h->d_mask, (size_t)h->nxw * ny * nz))) return rc;
+  if (!chan)
+    CK_CUDA(cudaMemcpyAsync(h->d_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice,
+                            h->stream));
   if ((rc = dev_alloc_t(h, &h->d_links, links.size() + 1))) return rc;
   if (!links.empty())
     CK_CUDA(cudaMemcpyAsync(h->d_links, links.data(), links.size() * sizeof(int4),
@@ -491,25 +390,59 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   CK_CUDA(cudaMemsetAsync(h->d_hist, 0, 3 * sizeof(double) * h->hist_cap, h->stream));
   if ((rc = dev_alloc_t(h, &h->d_step, 1))) return rc;
   CK_CUDA(cudaMemsetAsync(h->d_step, 0, sizeof(long long), h->stream));
-  h->link_blocks = (int)std::min<long long>(std::max<long long>((h->n_links + 255) / 256, 1), 1024);
   h->reduce_blocks = (int)std::min<long long>(std::max<long long>(((long long)N + 255) / 256, 1), 2048);
-  if (cfg->profile == CFLBM_PROFILE_CHANNEL) {
-    const std::vector<uint32_t> bits =
-        d3 ? channel_links<27>(solid, nx, ny, nz, cfg->wall_y, cfg->wall_z)
-           : channel_links<9>(solid, nx, ny, nz, cfg->wall_y, cfg->wall_z);
-    std::vector<int> list;
-    std::vector<uint32_t> tile_bits;
-    const std::vector<unsigned char> flag =
-        solid_tiles(solid, bits, nx, ny, nz, h->nxw, list, tile_bits);
-    h->n_slow = (int)list.size();
-    if ((rc = dev_alloc_t(h, &h->d_tile_slow, flag.size()))) return rc;
-    CK_CUDA(cudaMemcpyAsync(h->d_tile_slow, flag.data(), flag.size(), cudaMemcpyHostToDevice,
-                            h->stream));
-    std::vector<int> index(flag.size(), -1);
-    for (size_t t = 0; t < list.size(); ++t) index[(size_t)list[t]] = (int)t;
-    if ((rc = dev_alloc_t(h, &h->d_tile_index, index.size()))) return rc;
-    CK_CUDA(cudaMemcpyAsync(h->d_tile_index, index.data(), index.size() * sizeof(int),
-                            cudaMemcpyHostToDevice, h->stream));
+  if (chan) {
+    // Mask, per-cell link bits, listed tiles and their link words on the GPU
+    // (setup.cu); scratch: the link bits of every cell and an explicit mask's
+    // bytes, freed before returning.
+    SetupArgs sa{};
+    sa.nx = nx;
+    sa.ny = ny;
+    sa.nz = nz;
+    sa.nxw = h->nxw;
+    sa.wall_y = cfg->wall_y;
+    sa.wall_z = cfg->wall_z;
+    sa.geom = cfg->geom;
+    sa.cx = cfg->cx;
+    sa.cy = cfg->cy;
+    sa.cz = cfg->cz;
+    sa.r2 = 0.25 * cfg->diam * cfg->diam;
+    const size_t ntiles = (size_t)h->nxw * ny * nz;
+    const int nchunks = setup_chunks(sa);
+    // one scratch block: counters, chunk offsets + total, per-cell bits, input mask
+    const size_t off_chunk = 64, off_bits = off_chunk + 4 * ((size_t)nchunks + 16);
+    const size_t off_in = off_bits + 4 * N + 256;
+    const size_t scratch_bytes = off_in + (cfg->solid ? N : 0);
+    unsigned char *scratch = nullptr;
+    CK_CUDA(cudaMalloc(&scratch, scratch_bytes));
+    std::unique_ptr<unsigned char, cudaError_t (*)(void *)> scratch_guard(scratch, cudaFree);
+    unsigned long long *counters = reinterpret_cast<unsigned long long *>(scratch);
+    int *chunk = reinterpret_cast<int *>(scratch + off_chunk);
+    int *d_total = chunk + nchunks;
+    uint32_t *bits = reinterpret_cast<uint32_t *>(scratch + ((off_bits + 255) / 256) * 256);
+    CK_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), h->stream));
+    if (cfg->solid) {
+      uint8_t *in = scratch + off_in;
+      CK_CUDA(cudaMemcpyAsync(in, cfg->solid, N, cudaMemcpyHostToDevice, h->stream));
+      sa.solid_in = in;
+    }
+    if ((rc = dev_alloc_t(h, &h->d_tile_slow, ntiles))) return rc;
+    if ((rc = dev_alloc_t(h, &h->d_tile_index, ntiles))) return rc;
+    CK_CUDA(launch_setup_mask_links(Q, sa, h->d_mask, bits, counters, h->stream));
+    CK_CUDA(launch_setup_flags(sa, h->d_mask, bits, h->d_tile_slow, chunk, d_total, h->stream));
+    unsigned long long cnt[2] = {0, 0};
+    int total = 0;
+    CK_CUDA(cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream));
+    CK_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK_CUDA(cudaStreamSynchronize(h->stream));
+    h->n_solid = (long long)cnt[0];
+    h->n_links = (long long)cnt[1];
+    h->n_slow = total;
+    if ((rc = dev_alloc_t(h, &h->d_slow_tiles, (size_t)total + 1))) return rc;
+    if ((rc = dev_alloc_t(h, &h->d_links_bits, 32 * (size_t)total + 32))) return rc;
+    CK_CUDA(launch_setup_list(sa, h->d_tile_slow, chunk, h->d_mask, bits, h->d_tile_index,
+                              h->d_slow_tiles, h->d_links_bits, h->stream));
+    CK_CUDA(cudaStreamSynchronize(h->stream));  // the scratch is freed at scope end
     std::vector<long long> foff;
     std::vector<uint32_t> fbb;
     if (d3) face_tables<27>(L, cfg->wall_y, cfg->wall_z, foff, fbb);
@@ -520,15 +453,6 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
                             cudaMemcpyHostToDevice, h->stream));
     CK_CUDA(cudaMemcpyAsync(h->d_face_bb, fbb.data(), fbb.size() * sizeof(uint32_t),
                             cudaMemcpyHostToDevice, h->stream));
-    if ((rc = dev_alloc_t(h, &h->d_slow_tiles, list.size() + 1))) return rc;
-    if ((rc = dev_alloc_t(h, &h->d_links_bits, tile_bits.size() + 32))) return rc;
-    if (!list.empty()) {
-      CK_CUDA(cudaMemcpyAsync(h->d_slow_tiles, list.data(), list.size() * sizeof(int),
-                              cudaMemcpyHostToDevice, h->stream));
-      CK_CUDA(cudaMemcpyAsync(h->d_links_bits, tile_bits.data(), tile_bits.size() * 4,
-                              cudaMemcpyHostToDevice, h->stream));
-    }
-    CK_CUDA(cudaStreamSynchronize(h->stream));
     for (int i = 0; i < Q; ++i) {
       const int ex = d3 ? Lat<27>::ex(i) : Lat<9>::ex(i);
       const double w = d3 ? Lat<27>::w(i) : Lat<9>::w(i);
@@ -537,6 +461,7 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     }
     CK_CUDA(cudaStreamSynchronize(h->stream));  // host vectors die at scope end
   }
+  h->link_blocks = (int)std::min<long long>(std::max<long long>((h->n_links + 255) / 256, 1), 1024);
   // Force partials: one per block of listed tiles, for any tile height >= 1.
   const size_t nparts = std::max<size_t>(4 * (size_t)std::max(h->link_blocks, h->reduce_blocks),
                                          3 * (size_t)std::max(h->n_slow, 1));

@@ -80,8 +80,7 @@ int ref2d_setup(int nx, int ny, double u0, const int32_t *ran, RefSetup &out);
 int ref3d_setup(int nx, int ny, int nz, double u0, const int32_t *ran, RefSetup &out);
 int ref2ds_setup(int nx, int ny, double u0, const int32_t *ran, RefSetup &out);
 
-// Channel mask from the configured geometry (reference_setup.cpp).
-void channel_mask(const cflbm_config &c, std::vector<uint8_t> &solid);
+// Cd/Cl reference area of a channel's body (reference_setup.cpp).
 double channel_area(const cflbm_config &c);
 
 // Channel-sweep arguments of a handle (api.cu).

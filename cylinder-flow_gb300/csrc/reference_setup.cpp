@@ -124,28 +124,6 @@ int ref3d_setup(int nx, int ny, int nz, double u0, const int32_t *ran, RefSetup 
   return 0;
 }
 
-void channel_mask(const cflbm_config &c, std::vector<uint8_t> &solid) {
-  const int nz = c.lattice == CFLBM_D2Q9 ? 1 : c.nz;
-  const size_t N = (size_t)c.nx * c.ny * nz;
-  solid.assign(N, 0);
-  if (c.solid) {
-    for (size_t n = 0; n < N; ++n) solid[n] = c.solid[n] ? 1 : 0;
-    return;
-  }
-  if (c.geom != CFLBM_GEOM_CYLINDER && c.geom != CFLBM_GEOM_SPHERE) return;
-  const double r2 = 0.25 * c.diam * c.diam;
-  host_parallel_rows((long long)c.ny * nz, [&](long long r) {
-    const int y = (int)(r % c.ny), z = (int)(r / c.ny);
-    for (int x = 0; x < c.nx; ++x) {
-      const double dx = x - c.cx, dy = y - c.cy, dz = z - c.cz;
-      bool s = false;
-      if (c.geom == CFLBM_GEOM_CYLINDER) s = dx * dx + dy * dy <= r2;
-      else s = dx * dx + dy * dy + dz * dz <= r2;
-      solid[(size_t)r * c.nx + x] = s ? 1 : 0;
-    }
-  });
-}
-
 double channel_area(const cflbm_config &c) {
   const double D = c.diam > 0 ? c.diam : 1.0;
   if (c.geom == CFLBM_GEOM_SPHERE) return M_PI * D * D / 4.0;

@@ -20,8 +20,8 @@
 // x = nx - 1 for e_x < 0.  Cells of a listed tile with solid links take the
 // bounced population f*_opp(I)(X) from global memory (a few thousand cells per
 // step); solid cells get p = u = 0.  The arithmetic is channel2_cells' (packed
-// FP32x2, two cells per thread: x and x + 256), so the states are bit-identical
-// to the register-fed kernel's.
+// FP32x2, two cells per thread: x and x + 32 of a 64-cell warp span), so the
+// states are bit-identical to the register-fed kernel's.
 //
 // One thread of the block waits for a stage's copies (bounded) and the block
 // meets it at one barrier per line, which also orders the reads of the stage
@@ -33,7 +33,7 @@
 
 namespace cflbm {
 
-constexpr int LINES_THREADS = 256;           // two cells per thread: x and x + 256
+constexpr int LINES_THREADS = 256;           // two cells per thread: x and x + 32
 constexpr int LINES_CELLS = 2 * LINES_THREADS;
 constexpr unsigned LINES_TIMEOUT = 0x4C494E45u;  // error word ("LINE")
 constexpr long long LINES_SPIN_LIMIT = 1LL << 22;  // try_wait polls (~seconds) before giving up
@@ -178,8 +178,10 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
     const unsigned wbb = s_bb[st];
     const long long rowc = a.L.idx(0, y, z);  // cell x = 0, population 0
     for (int xb = 0; xb < nx; xb += LINES_CELLS) {
-      const int x0 = xb + tid, x1 = x0 + LINES_THREADS;
-      if (xb + 32 * (tid >> 5) >= nx) continue;  // warp entirely past the line
+      // warp w takes the tiles 2w and 2w + 1 of this 512-cell block: cells x0
+      // and x0 + 32, the pairs of the register-fed kernel (same rounding keys)
+      const int x0 = xb + 64 * (tid >> 5) + lane, x1 = x0 + 32;
+      if (xb + 64 * (tid >> 5) >= nx) continue;  // warp entirely past the line
       const bool st0 = x0 < nx, st1 = x1 < nx;
       // listed tiles of the warp's two 32-cell tiles (solid cells or links)
       const long long trow = ((long long)z * ny + y) * a.nxw;
@@ -226,7 +228,8 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
       E *__restrict__ q = static_cast<E *>(a.fb) + rowc;
 #pragma unroll
       for (int i = 0; i < Q; ++i)
-        PairCodec<ST>::put2(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i], a.L.fbase[i], st0, st1);
+        PairCodec<ST>::put2(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i], a.L.fbase[i], st0, st1,
+                            (unsigned)((ln * nx + x0) * Q + i));
     }
     // the next line's stage: thread 0 waits for its copies, then the barrier
     // (which also orders every read of stage s before its refill)

@@ -285,7 +285,9 @@ int cflbm_get_timing(cflbm_handle *h, double ms[2], int64_t counts[2]);
  * array of 512 KiB held by every GPU that loads the library until exit; grids of
  * more than 134,217,728 cells are rejected with CFLBM_E_INVALID.  The first call
  * on a device looks up the array's device address; make it before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race.
+ * capture.  The address is kept for the process, so the call serves the
+ * device's primary context only: not after cudaDeviceReset, not from another
+ * driver context.  Calls share the array, so calls that overlap on the GPU race.
  * Asynchronous: read d_out after synchronising the stream. */
 int cflbm_domain_sums_noalloc(int lattice, int storage, int nx, int ny, int nz,
                               const void *d_f, const uint8_t *d_solid, double *d_out,
