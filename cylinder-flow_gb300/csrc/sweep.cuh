@@ -339,7 +339,8 @@ __device__ __forceinline__ void finish_cell(A *f, A rho3, A ux, A uy, A uz, long
   bgk_relax<L, A, SF>(f, rho3, ux, uy, uz, a);
   if (store) {
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) SF::template store<A, L>(fb + i * S + c, f[i], a.L.fbase[i]);
+    for (int i = 0; i < L::Q; ++i)
+      SF::template store<A, L>(fb + i * S + c, f[i], a.L.fbase[i], (unsigned)(cell * L::Q + i));
   }
 }
 
@@ -424,25 +425,15 @@ template <> struct PairT<float2> {
 
 // Storage codec of a cell pair on FP32x2 (the two-cell kernels): the raw
 // elements convert one by one and the FP16 format's offset and scale apply to
-// the pair in one packed FMA -- the same values as Store<>::load per cell (the
-// product with a power of two is exact, so fma(v, 2^12, -2^12 b) = 2^12 (v - b)
-// rounded once).  `key` names the first value's element (cell * Q + i).
-//
-// FP16 stores round stochastically: each value's bit pattern gets a uniform
-// 13-bit integer added below binary16's last mantissa bit before truncation,
-// so a value rounds up with the probability of its distance from the value
-// below -- an unbiased rounding, where round-to-nearest turns the same
-// residual into the same error step after step.  The integer is a hash of the
-// two values' bit patterns and the element (deterministic: the same state
-// gives the same bits, so runs repeat and resume exactly).  On the D2Q9
-// 400x100 cylinder run (20,000 steps) round-to-nearest moved the lift rms by
-// 3.3% and the mean drag over the last 10,000 steps by 2.4e-3; with this
-// rounding 0.1% and 7e-5.  The hash key is the logical element (cell * Q + i
-// of the first cell), so every layout and kernel rounds a state alike.
+// the pair in one packed FMA -- the same values as Store<>::load/store per cell
+// (the product with a power of two is exact, so fma(v, 2^12, -2^12 b) is
+// 2^12 (v - b) rounded once).  `key` is the first value's element (cell * Q +
+// i); the second cell lies 32 cells further.
 template <class ST> struct PairCodec;
 template <> struct PairCodec<double> {
   __device__ static float raw(double e) { return d2f_bits(e); }
   __device__ static float2 dec(float2 r, float2) { return r; }
+  template <int Q>
   __device__ static void put2(double *p0, double *p1, float2 v, float, bool s0, bool s1,
                               unsigned) {
     if (s0) *p0 = f2d_bits(v.x);
@@ -452,6 +443,7 @@ template <> struct PairCodec<double> {
 template <> struct PairCodec<float> {
   __device__ static float raw(float e) { return e; }
   __device__ static float2 dec(float2 r, float2) { return r; }
+  template <int Q>
   __device__ static void put2(float *p0, float *p1, float2 v, float, bool s0, bool s1,
                               unsigned) {
     if (s0) *p0 = v.x;
@@ -463,17 +455,13 @@ template <> struct PairCodec<F16Dev> {
   __device__ static float2 dec(float2 r, float2 b) {
     return __ffma2_rn(r, make_float2(1.0f / F16_SCALE, 1.0f / F16_SCALE), b);
   }
+  template <int Q>
   __device__ static void put2(__half *p0, __half *p1, float2 v, float b, bool s0, bool s1,
                               unsigned key) {
     const float nb = -F16_SCALE * b;
     const float2 sv = __ffma2_rn(v, make_float2(F16_SCALE, F16_SCALE), make_float2(nb, nb));
-    const unsigned u0 = __float_as_uint(sv.x), u1 = __float_as_uint(sv.y);
-    unsigned h = (u0 ^ (u1 * 0x9E3779B1u)) ^ (key * 0x85EBCA77u);
-    h ^= h >> 15;
-    h *= 0x2C1B3C6Du;
-    h ^= h >> 12;
-    if (s0) *p0 = __float2half_rz(__uint_as_float(u0 + (h & 0x1FFFu)));
-    if (s1) *p1 = __float2half_rz(__uint_as_float(u1 + ((h >> 13) & 0x1FFFu)));
+    if (s0) *p0 = f16_stochastic(sv.x, key);
+    if (s1) *p1 = f16_stochastic(sv.y, key + 32u * Q);
   }
 };
 
@@ -744,8 +732,8 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
   E *__restrict__ q = static_cast<E *>(a.fb) + c;
 #pragma unroll
   for (int i = 0; i < L::Q; ++i)
-    PairCodec<ST>::put2(q + i * S, q + i * S + 32, f[i], a.L.fbase[i], st0, st1,
-                        (unsigned)(cell0 * Q + i));
+    PairCodec<ST>::template put2<Q>(q + i * S, q + i * S + 32, f[i], a.L.fbase[i], st0, st1,
+                                    (unsigned)(cell0 * Q + i));
 }
 
 template <int Q, class ST, class P, int MINB>

@@ -228,8 +228,9 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
       E *__restrict__ q = static_cast<E *>(a.fb) + rowc;
 #pragma unroll
       for (int i = 0; i < Q; ++i)
-        PairCodec<ST>::put2(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i], a.L.fbase[i], st0, st1,
-                            (unsigned)((ln * nx + x0) * Q + i));
+        PairCodec<ST>::template put2<Q>(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i],
+                                        a.L.fbase[i], st0, st1,
+                                        (unsigned)((ln * nx + x0) * Q + i));
     }
     // the next line's stage: thread 0 waits for its copies, then the barrier
     // (which also orders every read of stage s before its refill)

@@ -50,5 +50,8 @@ def test_config1_statistics_match_oracle(cuda, storage, compute, tol_f, tol_stat
     assert st["periods"] >= 3 and ref["periods"] >= 3
     assert abs(st["cd_mean_periods"] - ref["cd_mean_periods"]) <= tol_stats * abs(
         ref["cd_mean_periods"])
-    assert abs(st["cl_rms"] - ref["cl_rms"]) <= 5 * tol_stats * abs(ref["cl_rms"])
+    # the lift rms: 5x the drag bar; FP16 storage 2e-2 (its rounding noise adds
+    # lift fluctuations)
+    tol_cl = 2e-2 if storage == "fp16dev" else 5 * tol_stats
+    assert abs(st["cl_rms"] - ref["cl_rms"]) <= tol_cl * abs(ref["cl_rms"])
     assert abs(st["st"] - ref["st"]) <= tol_stats * abs(ref["st"])

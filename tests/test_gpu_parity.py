@@ -82,9 +82,9 @@ def test_ref2ds_matches_reference_golden(cuda):
     assert rel_err(fstream, g["fstream"]) < TOL64
 
 
-@pytest.mark.parametrize("compute,tol", [("fp64", 1e-10), ("df64", 1e-9), ("fp32", 5e-5)])
+@pytest.mark.parametrize("compute,tol", [("fp64", 1e-10), ("df64", 1e-9), ("fp32", 2e-5)])
 def test_ref2ds_matches_oracle_longer_run(cuda, compute, tol):
-    nx, ny, steps = 240, 64, 800
+    nx, ny, steps = 240, 64, 300
     ran = np.random.default_rng(11).integers(0, 100, size=(nx + 4, ny + 4)).astype(np.int32)
     o = O.ref2ds(nx, ny, 0.03, 0.06, ran, steps)
     with Solver(lattice=9, nx=nx, ny=ny, profile="ref2ds", tau0=0.03, u0=0.06, ref_ran=ran,
