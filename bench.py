@@ -186,10 +186,11 @@ def form_errors(s, oracle_run):
             "p": rel(p, o["p"]), "fx": abs(fh[-1, 0] - o["force"][-1, 0]) / abs(o["force"][-1, 0])}
 
 
-def variant(cflbm, local, storage, compute, layout, steps, warmup, oracle_run):
+def variant(cflbm, local, storage, compute, layout, steps, warmup, oracle_run,
+            rounding="nearest"):
     import torch
     with cflbm.Solver(device=local, storage=storage, compute=compute, layout=layout,
-                      **WORKLOAD) as s:
+                      rounding=rounding, **WORKLOAD) as s:
         err = None
         if oracle_run is not None:
             s.step(ERR_STEPS)
@@ -265,8 +266,10 @@ def run_gb300(args):
                                   ("fp32_store", "fp32", "fp32", "rows"),
                                   ("fp32_store_soa", "fp32", "fp32", "soa"),
                                   ("fp16dev_store", "fp16dev", "fp32", "rows"),
-                                  ("fp16dev_store_soa", "fp16dev", "fp32", "soa")):
-            v = variant(cflbm, local, st, cp, lay, steps, min(warmup, 5), oracle_run)
+                                  ("fp16dev_store_soa", "fp16dev", "fp32", "soa"),
+                                  ("fp16dev_sr_store_soa", "fp16dev", "fp32", "soa")):
+            v = variant(cflbm, local, st, cp, lay, steps, min(warmup, 5), oracle_run,
+                        "stochastic" if "_sr_" in name else "nearest")
             v["hbm_frac"] = v["bytes_per_cell"] * CELLS / (v["sweep_us"] * 1e-6) / 1e9 / peak
             extra[name] = {k: (round(x, 4) if isinstance(x, float) else x) for k, x in v.items()}
 
@@ -367,8 +370,10 @@ def run_channel2d(args):
     with ClockSampler(local) as clk:
         for name, st, cp in (("fp64", "fp64", "fp64"), ("df64", "fp64", "df64"),
                              ("fp64_store", "fp64", "fp32"), ("fp32_store", "fp32", "fp32"),
-                             ("fp16dev_store", "fp16dev", "fp32")):
+                             ("fp16dev_store", "fp16dev", "fp32"),
+                             ("fp16dev_sr_store", "fp16dev", "fp32")):
             with cflbm.Solver(device=local, storage=st, compute=cp, force_history=steps + 8,
+                              rounding="stochastic" if "_sr_" in name else "nearest",
                               **CH2D) as s:
                 stream = torch.cuda.ExternalStream(s.stream_ptr())
                 f0 = s.get_f()

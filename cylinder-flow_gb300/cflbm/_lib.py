@@ -19,6 +19,7 @@ PROFILE_CHANNEL, PROFILE_REF2D, PROFILE_REF3D, PROFILE_REF2DS = 0, 1, 2, 3
 WALL_FREESLIP, WALL_NOSLIP, WALL_PERIODIC = 0, 1, 2
 GEOM_NONE, GEOM_CYLINDER, GEOM_SPHERE = 0, 1, 2
 LAYOUT_SOA, LAYOUT_ROWS = 0, 1
+ROUND_NEAREST, ROUND_STOCHASTIC = 0, 1
 
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "numeric error",
           5: "I/O error", 6: "unsupported"}
@@ -37,6 +38,7 @@ class Config(ctypes.Structure):
         ("seed", ctypes.c_uint64), ("solid", ctypes.POINTER(ctypes.c_uint8)),
         ("alpha", _dp), ("ref_ran", ctypes.POINTER(ctypes.c_int32)),
         ("force_history", ctypes.c_int), ("device", ctypes.c_int), ("layout", ctypes.c_int),
+        ("rounding", ctypes.c_int),
     ]
 
 

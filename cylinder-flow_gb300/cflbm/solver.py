@@ -35,6 +35,7 @@ class Solver:
                    "periodic": C.WALL_PERIODIC},
         "geom": {"none": C.GEOM_NONE, "cylinder": C.GEOM_CYLINDER, "sphere": C.GEOM_SPHERE},
         "layout": {"soa": C.LAYOUT_SOA, "rows": C.LAYOUT_ROWS},
+        "rounding": {"nearest": C.ROUND_NEAREST, "stochastic": C.ROUND_STOCHASTIC},
     }
 
     def __init__(self, **kw):

@@ -2,12 +2,20 @@
 
 precision_study: one problem run with FP64 arithmetic on FP64 storage (the
 reference arithmetic, used as the FP64 oracle at sizes the CPU oracle cannot
-reach) and with FP32 arithmetic on FP64, FP32 and FP16-deviation storage.  For
-each form it reports the sweep's MLUPS and HBM fraction, the final u field's
-error against the FP64 run, the mean drag coefficient, its error, the lift rms,
-the Strouhal number and the FP64 mass drift.
+reach), with double-float (DF64) arithmetic on FP64 storage, and with FP32
+arithmetic on FP64, FP32 and FP16-deviation storage.  For each form it reports
+the sweep's MLUPS and HBM fraction, the final u field's error against the FP64
+run, the mean drag coefficient (plain window mean and the mean over whole
+shedding periods), their errors, the lift rms, the Strouhal number and the
+FP64 mass drift.
 
     python -m cflbm.studies precision --nx 768 --ny 384 --nz 384 --steps 20000
+    python -m cflbm.studies precision --case channel2d --steps 40000 --window 10000
+
+The second line is the D2Q9 400x100 cylinder channel (Re 100) run to its
+periodic state: its shedding grows until about step 28,000, so drag averaged
+over steps 10,000-20,000 also measures when the shedding set in (which round-off
+noise moves), while steps 30,000-40,000 measure the periodic state itself.
 
 adjoint_study: the differentiation problem (D2Q9 1024x256 channel, cylinder
 D=32 at (200, 128), porosity on a 128x128 box, mean drag over steps 5000-7000
@@ -49,24 +57,35 @@ def measured_peak_gbs() -> float:
     return 6800.0
 
 
-FORMS = [  # name, storage, compute
-    ("fp64_arith", "fp64", "fp64"),
-    ("fp64_store", "fp64", "fp32"),
-    ("fp32_store", "fp32", "fp32"),
-    ("fp16dev_store", "fp16dev", "fp32"),
+FORMS = [  # name, storage, compute, FP16 rounding
+    ("fp64_arith", "fp64", "fp64", "nearest"),
+    ("df64_arith", "fp64", "df64", "nearest"),
+    ("fp64_store", "fp64", "fp32", "nearest"),
+    ("fp32_store", "fp32", "fp32", "nearest"),
+    ("fp16dev_store", "fp16dev", "fp32", "nearest"),
+    ("fp16dev_sr_store", "fp16dev", "fp32", "stochastic"),
 ]
 
 
-def sphere_case(nx=768, ny=384, nz=384, diam=64.0, u0=0.03, re=300.0):
+def sphere_case(nx=768, ny=384, nz=384, diam=64.0, u0=0.03, re=300.0, seed=1234):
     """The precision-form problem: a sphere in a free-slip box."""
     return dict(lattice=27, nx=nx, ny=ny, nz=nz, tau0=3.0 * u0 * diam / re, u0=u0,
                 wall_y="freeslip", wall_z="freeslip", geom="sphere", cx=nx / 4.0,
-                cy=ny / 2.0, cz=nz / 2.0, diam=diam, perturb_amp=1e-3, seed=1234)
+                cy=ny / 2.0, cz=nz / 2.0, diam=diam, perturb_amp=1e-3, seed=seed)
 
 
-def run_form(case, storage, compute, steps, window, peak_gbs, chunk=1000, timing_steps=20):
+def channel2d_case(nx=400, ny=100, diam=20.0, u0=0.05, re=100.0, seed=1234):
+    """The small benchmark problem: a cylinder at (80, 50) in a free-slip channel."""
+    return dict(lattice=9, nx=nx, ny=ny, nz=1, tau0=3.0 * u0 * diam / re, u0=u0,
+                wall_y="freeslip", geom="cylinder", cx=nx / 5.0, cy=ny / 2.0, diam=diam,
+                perturb_amp=1e-3, seed=seed)
+
+
+def run_form(case, storage, compute, steps, window, peak_gbs, chunk=1000, timing_steps=20,
+             rounding="nearest"):
     out = {}
-    with Solver(storage=storage, compute=compute, force_history=steps + 8, **case) as s:
+    with Solver(storage=storage, compute=compute, rounding=rounding, force_history=steps + 8,
+                **case) as s:
         info = s.info()
         m0, _ = s.mass()
         t0 = time.perf_counter()
@@ -100,15 +119,16 @@ def run_form(case, storage, compute, steps, window, peak_gbs, chunk=1000, timing
 def precision_study(case, steps, window, peak_gbs, forms=FORMS, out_path=None):
     results = {"case": case, "steps": steps, "window": window, "forms": {}}
     u_ref = None
-    cd_ref = None
-    for name, storage, compute in forms:
-        r, u = run_form(case, storage, compute, steps, window, peak_gbs)
+    ref = None
+    for name, storage, compute, rounding in forms:
+        r, u = run_form(case, storage, compute, steps, window, peak_gbs, rounding=rounding)
         if u_ref is None:
-            u_ref, cd_ref = u, r["cd_mean"]
+            u_ref, ref = u, dict(r)
         r["u_err_linf"] = float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref)))
         r["u_err_l2"] = float(np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref))
-        r["cd_err_abs"] = float(abs(r["cd_mean"] - cd_ref))
-        r["cd_err_rel"] = float(abs(r["cd_mean"] - cd_ref) / abs(cd_ref))
+        for k in ("cd_mean", "cd_mean_periods", "cl_rms", "st"):
+            r[k + "_err_abs"] = float(abs(r[k] - ref[k]))
+            r[k + "_err_rel"] = float(abs(r[k] - ref[k]) / max(abs(ref[k]), 1e-300))
         results["forms"][name] = r
         del u
         if out_path:
@@ -300,6 +320,11 @@ def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=None,
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("study", choices=["precision", "adjoint", "batch"])
+    ap.add_argument("--case", choices=["sphere", "channel2d"], default="sphere",
+                    help="precision: the D3Q27 sphere box or the D2Q9 400x100 channel")
+    ap.add_argument("--seed", type=int, default=1234, help="precision: perturbation seed")
+    ap.add_argument("--layout", choices=["rows", "soa"], default=None,
+                    help="precision: population layout (default: the solver's)")
     ap.add_argument("--nx", type=int, default=768)
     ap.add_argument("--ny", type=int, default=384)
     ap.add_argument("--nz", type=int, default=384)
@@ -339,7 +364,13 @@ def main():
         return
     keep = set(args.forms.split(","))
     forms = [f for f in FORMS if f[0] in keep]
-    case = sphere_case(args.nx, args.ny, args.nz, diam=64.0 * args.nx / 768.0)
+    if args.case == "channel2d":
+        case = channel2d_case(seed=args.seed)
+    else:
+        case = sphere_case(args.nx, args.ny, args.nz, diam=64.0 * args.nx / 768.0,
+                           seed=args.seed)
+    if args.layout:
+        case["layout"] = args.layout
     precision_study(case, args.steps, args.window, args.peak, forms, args.out)
 
 

@@ -235,6 +235,8 @@ int validate(const cflbm_config *c) {
   if (c->force_history < 0) return fail(CFLBM_E_INVALID, "force_history < 0");
   if (c->layout != CFLBM_LAYOUT_SOA && c->layout != CFLBM_LAYOUT_ROWS)
     return fail(CFLBM_E_INVALID, "layout %d unknown", c->layout);
+  if (c->rounding != CFLBM_ROUND_NEAREST && c->rounding != CFLBM_ROUND_STOCHASTIC)
+    return fail(CFLBM_E_INVALID, "rounding %d unknown", c->rounding);
   return CFLBM_OK;
 }
 
@@ -263,6 +265,7 @@ int cflbm_config_default(cflbm_config *c) {
   c->geom = CFLBM_GEOM_NONE;
   c->seed = 1234;
   c->layout = CFLBM_LAYOUT_ROWS;
+  c->rounding = CFLBM_ROUND_NEAREST;
   return CFLBM_OK;
 }
 
@@ -561,25 +564,56 @@ namespace cflbm {
 void set_relax(SweepArgs &a, int Q, int, double omega) {
   a.omega = omega;
   a.omega_f = (float)omega;
-  double rk[13] = {1.0 - omega};
-  for (int c = 0; c <= (Q == 27 ? 3 : 2); ++c) {
-    // weight of class c (|e|^2 = c): the first direction of it
-    int i = 0;
-    for (int k = 0; k < Q; ++k) {
-      const int ex = Q == 27 ? Lat<27>::ex(k) : Lat<9>::ex(k);
-      const int ey = Q == 27 ? Lat<27>::ey(k) : Lat<9>::ey(k);
-      const int ez = Q == 27 ? Lat<27>::ez(k) : 0;
-      if (ex * ex + ey * ey + ez * ez == c) { i = k; break; }
-    }
-    const double kw = omega * (Q == 27 ? Lat<27>::w(i) : Lat<9>::w(i));
-    rk[1 + c] = kw;
-    rk[5 + c] = 4.5 * kw;
-    rk[9 + c] = 3.0 * kw;
+  // per weight class c = |e|^2: weight, directions, directions with e_x != 0
+  double w[4] = {};
+  int n[4] = {}, m[4] = {};
+  for (int k = 0; k < Q; ++k) {
+    const int ex = Q == 27 ? Lat<27>::ex(k) : Lat<9>::ex(k);
+    const int ey = Q == 27 ? Lat<27>::ey(k) : Lat<9>::ey(k);
+    const int ez = Q == 27 ? Lat<27>::ez(k) : 0;
+    const int c = ex * ex + ey * ey + ez * ez;
+    w[c] = Q == 27 ? Lat<27>::w(k) : Lat<9>::w(k);
+    ++n[c];
+    m[c] += ex * ex;
   }
-  for (int k = 0; k < 13; ++k) {
+  const int NC = Q == 27 ? 4 : 3;
+  double rk[RK_N] = {1.0 - omega};
+  for (int c = 0; c < NC; ++c) {
+    rk[RK_W + c] = omega * w[c];
+    rk[RK_A + c] = 4.5 * omega * w[c];
+    rk[RK_3 + c] = 3.0 * omega * w[c];
+  }
+  // FP32: Om = 1 - float(1 - omega) exactly; every class from Om, then the rest
+  // class's Kw and the face class's K3, Ka recomputed so that the identities
+  // hold exactly (the sums below are exact in FP64: few terms of 24-bit values
+  // spanning < 32 binades) and split into FP32 pairs (hi + lo exact).
+  float kf[RK_N] = {};
+  kf[RK_OMC] = (float)(1.0 - omega);
+  const double Om = 1.0 - (double)kf[RK_OMC];
+  for (int c = 0; c < NC; ++c) {
+    kf[RK_W + c] = (float)(Om * w[c]);
+    kf[RK_A + c] = (float)(4.5 * Om * w[c]);
+    kf[RK_3 + c] = (float)(3.0 * Om * w[c]);
+  }
+  double kw0 = Om, k31 = Om, ka1 = 1.5 * Om;
+  for (int c = 1; c < NC; ++c) kw0 -= n[c] * (double)kf[RK_W + c];
+  for (int c = 2; c < NC; ++c) {
+    k31 -= m[c] * (double)kf[RK_3 + c];
+    ka1 -= m[c] * (double)kf[RK_A + c];
+  }
+  k31 /= m[1];
+  ka1 /= m[1];
+  auto split = [&](double x, int hi, int lo) {
+    kf[hi] = (float)x;
+    kf[lo] = (float)(x - (double)kf[hi]);
+  };
+  split(kw0, RK_W, RK_LW);
+  split(k31, RK_3 + 1, RK_L3);
+  split(ka1, RK_A + 1, RK_LA);
+  for (int k = 0; k < RK_N; ++k) {
     a.rk[k] = rk[k];
-    a.rkf[k] = (float)rk[k];
-    a.rkl[k] = (float)(rk[k] - (double)a.rkf[k]);
+    a.rkf[k] = kf[k];
+    a.rkl[k] = (float)(rk[k] - (double)kf[k]);
   }
 }
 
@@ -592,6 +626,7 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   sa.mask = h->d_mask;
   sa.nxw = h->nxw;
   set_relax(sa, h->Q, h->cfg.storage, h->omega);
+  sa.f16_sr = h->cfg.rounding == CFLBM_ROUND_STOCHASTIC;
   sa.alpha = h->d_alpha;
   if (write_macros) {
     sa.mu = h->d_mu;
@@ -707,6 +742,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   sa.mask = h->d_mask;
   sa.nxw = h->nxw;
   set_relax(sa, Q, st, h->omega);
+  sa.f16_sr = h->cfg.rounding == CFLBM_ROUND_STOCHASTIC;
   sa.ref_override = ref ? 1 : 0;
   sa.inlet_u = h->d_inlet;
   sa.alpha = h->d_alpha;

@@ -6,11 +6,18 @@
 namespace cflbm {
 
 namespace {
-// Ring depth and blocks per SM for a line of nx cells: two blocks per SM when
-// two rings of two stages fit in 200 KB of shared memory, the deepest ring (up
-// to 4 stages) that fits beside the other block.
+// Bytes of one ring stage for a line of nx cells: the Q staged rows, the link
+// words and positions of the line's tiles, rounded up to 128 bytes.
+size_t stage_bytes(int nx, int elem) {
+  const size_t nxw_pad = ((size_t)(nx + 31) / 32 + 3) / 4 * 4;
+  const size_t b = (size_t)27 * lines_window(nx) * elem + nxw_pad * (32 * 4 + 4);
+  return (b + 127) / 128 * 128;
+}
+// Ring depth and blocks per SM: two blocks per SM when two rings of two stages
+// fit in 200 KB of shared memory, the deepest ring (up to 4 stages) that fits
+// beside the other block.
 void lines_shape(int nx, int elem, int &stages, int &per_sm, size_t &smem) {
-  const size_t stage = (size_t)27 * lines_window(nx) * elem;
+  const size_t stage = stage_bytes(nx, elem);
   const size_t budget = 200u * 1024u;
   per_sm = (4 * stage <= budget) ? 2 : 1;
   stages = (int)std::min<size_t>(4, budget / per_sm / stage);
@@ -42,10 +49,12 @@ cudaError_t launch_lines_f16_q27(const SweepArgs &a, int sms, cudaStream_t s) {
   LinesArgs la{};
   la.stages = stages;
   la.window = lines_window(a.L.nx);
+  la.nxw_pad = (a.nxw + 3) / 4 * 4;
   la.lines = (long long)a.L.ny * a.L.nz;
+  la.stage_bytes = stage_bytes(a.L.nx, 2);
   la.err = a.err;
   const long long grid = std::min<long long>(la.lines, (long long)sms * per_sm);
-  sweep_lines_kernel<27, F16Dev, 2><<<(unsigned)grid, LINES_THREADS, smem, s>>>(a, la);
+  sweep_lines_kernel<27, F16Dev, 2><<<(unsigned)grid, LINES_THREADS + 32, smem, s>>>(a, la);
   return cudaGetLastError();
 }
 

@@ -51,6 +51,10 @@ __host__ __device__ inline bool mask_solid(const uint32_t *m, int nxw, int ny, i
   return (m[((long long)z * ny + y) * nxw + (x >> 5)] >> (x & 31)) & 1u;
 }
 
+// Indices of the relaxation constants (their meaning: bgk_relax_v, sweep.cuh).
+constexpr int RK_OMC = 0, RK_W = 1, RK_A = 5, RK_3 = 9, RK_LW = 13, RK_L3 = 14, RK_LA = 15,
+              RK_N = 16;
+
 struct SweepArgs {
   Layout L;
   const void *fa;        // post-collision state of this step (ghosts filled)
@@ -59,12 +63,13 @@ struct SweepArgs {
   int nxw;               // mask words per row
   float omega_f;
   double omega;
-  // Relaxation constants (1 - omega and omega times the weight-class factors,
-  // storage scale included; layout in sweep.cuh, RK_*): FP64, FP32, and the
-  // FP32 remainder rk - rkf for double-float arithmetic.
-  double rk[13];
-  float rkf[13];
-  float rkl[13];
+  // Relaxation constants (1 - omega and omega times the weight-class factors;
+  // layout in sweep.cuh, RK_*): FP64, the conserving FP32 set, and the FP32
+  // remainder rk - rkf for double-float arithmetic.
+  double rk[RK_N];
+  float rkf[RK_N];
+  float rkl[RK_N];
+  bool f16_sr;           // FP16 storage: stochastic rounding of stores (else nearest)
   int ref_override;      // reference profiles: inlet u at x = 0, p = 0 at x = nx-1
   const double *inlet_u; // ny*nz inlet velocity profile (reference profiles)
   const float *alpha;    // nx*ny*nz Brinkman porosity or null

@@ -23,17 +23,20 @@
 // FP32x2, two cells per thread: x and x + 32 of a 64-cell warp span), so the
 // states are bit-identical to the register-fed kernel's.
 //
-// One thread of the block waits for a stage's copies (bounded) and the block
-// meets it at one barrier per line, which also orders the reads of the stage
-// before its refill.  A wait that gives up records LINES_TIMEOUT in *a.err
-// (read by the host at the next synchronising call), waits (bounded) for the
-// copies the block has in flight, and returns.
+// A producer warp issues the copies (and the line's listed-tile positions and
+// link words) into a ring of stages; eight consumer warps compute.  Stages are
+// handed over with a full and an empty mbarrier each, so no block-wide barrier
+// couples the warps.  Every wait is bounded; a wait that gives up records
+// LINES_TIMEOUT in *a.err (read by the host at the next synchronising call);
+// the producer then waits (bounded) for the copies it issued, and the block
+// returns.
 #pragma once
 #include "sweep.cuh"
 
 namespace cflbm {
 
-constexpr int LINES_THREADS = 256;           // two cells per thread: x and x + 32
+constexpr int LINES_THREADS = 256;           // consumer threads, two cells each: x and x + 32
+static_assert(SWEEP_BX == 32, "a tile is one warp of cells, its link words one 128-byte copy");
 constexpr int LINES_CELLS = 2 * LINES_THREADS;
 constexpr unsigned LINES_TIMEOUT = 0x4C494E45u;  // error word ("LINE")
 constexpr long long LINES_SPIN_LIMIT = 1LL << 22;  // try_wait polls (~seconds) before giving up
@@ -80,115 +83,164 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
 }
 
 struct LinesArgs {
-  int stages;    // ring depth
-  int window;    // lines_window(nx) elements per staged row
+  int stages;       // ring depth
+  int window;       // lines_window(nx) elements per staged row
+  int nxw_pad;      // tiles of a line, rounded up to 4 (the stage's tile areas)
   long long lines;  // ny * nz
+  size_t stage_bytes;  // bytes per stage: rows, then link words, then tile positions
   unsigned *err;    // error word (0 = fine)
 };
 
-// Issue the Q bulk copies of line `ln` into stage buffer `buf` (one thread).
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// The producer warp: for line ln into stage buffer `st` -- the line's tile
+// positions (one per lane), the rows of every population and the link words
+// of its listed tiles, all completing on `full`.
 template <int Q, class E>
-__device__ __forceinline__ void lines_issue(const SweepArgs &a, const LinesArgs &la, long long ln,
-                                            E *buf, unsigned long long *bar,
-                                            const long long *face_off, const unsigned *face_bb) {
-  using L = Lat<Q>;
+__device__ __forceinline__ void lines_produce(const SweepArgs &a, const LinesArgs &la, long long ln,
+                                              unsigned char *st, unsigned long long *full,
+                                              const long long *row_off) {
+  const int lane = threadIdx.x & 31;
   const int ny = a.L.ny;
   const int y = (int)(ln % ny), z = (int)(ln / ny);
-  const int st = face_state(y, z, ny, a.L.nz);
-  const unsigned wbb = face_bb[st];
+  const int fs = face_state(y, z, ny, a.L.nz);
+  E *rows = reinterpret_cast<E *>(st);
+  uint32_t *links = reinterpret_cast<uint32_t *>(st + (size_t)Q * la.window * sizeof(E));
+  int *tiles = reinterpret_cast<int *>(links + (size_t)la.nxw_pad * 32);
+  const long long trow = (long long)ln * a.nxw;
+  // tile positions in the list (-1: not listed), and how many are listed
+  int listed = 0;
+  for (int w0 = 0; w0 < a.nxw; w0 += 32) {
+    const int w = w0 + lane;
+    const int t = w < a.nxw ? a.tile_index[trow + w] : -1;
+    if (w < a.nxw) tiles[w] = t;
+    listed += __popc(__ballot_sync(0xffffffffu, t >= 0));
+  }
+  const unsigned row_bytes = (unsigned)(la.window * sizeof(E));
+  __syncwarp();
+  if (lane == 0) {
+    // order this block's earlier generic reads of the stage before the async writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(full, row_bytes * Q + 128u * (unsigned)listed);
+  }
+  __syncwarp();
   const E *fa = static_cast<const E *>(a.fa);
   const long long line0 = a.L.idx(0, y, z) - a.L.xoff;  // element 0 of population 0's row
-  const unsigned bytes = (unsigned)(la.window * sizeof(E));
-  // order this block's earlier generic reads of the stage before the async writes
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  mbar_expect_tx(bar, bytes * Q);
-#pragma unroll
-  for (int I = 0; I < Q; ++I) {
-    long long row;
-    if (I == 0) row = line0;
-    else if ((wbb >> I) & 1u) row = line0 + (long long)L::opp(I) * a.L.S;
-    else row = line0 + face_off[st * Q + I] + L::ex(I);  // undo the table's x shift
-    bulk_copy_g2s(buf + (size_t)I * la.window, fa + row + a.L.xoff - 8, bytes, bar);
+  for (int I = lane; I < Q; I += 32)
+    bulk_copy_g2s(rows + (size_t)I * la.window, fa + line0 + row_off[fs * Q + I] + a.L.xoff - 8,
+                  row_bytes, full);
+  for (int w = lane; w < a.nxw; w += 32) {
+    const int t = tiles[w];
+    if (t >= 0) bulk_copy_g2s(links + (size_t)w * 32, a.links_bits + (long long)t * SWEEP_BX, 128u, full);
   }
 }
 
+// Block: LINES_THREADS consumer threads (8 warps, two cells each per 512-cell
+// block of a line) and one producer warp.  Stage s is handed over with two
+// mbarriers: full[s] completes when the stage's copies have landed, empty[s]
+// when every consumer warp is done with it.  No block-wide barrier in the loop:
+// each warp waits only for the data it reads.
 template <int Q, class ST, int MINB>
-__global__ void __launch_bounds__(LINES_THREADS, MINB)
+__global__ void __launch_bounds__(LINES_THREADS + 32, MINB)
     sweep_lines_kernel(const SweepArgs a, const LinesArgs la) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
   extern __shared__ __align__(128) unsigned char lines_smem[];
-  __shared__ unsigned long long bars[4];
-  __shared__ int failed;
-  __shared__ long long s_off[16 * Q];  // the face-state tables, for the issuing thread
+  __shared__ unsigned long long full[4], empty[4];
+  __shared__ volatile int failed;
+  // per face state and direction: the source row relative to the line's
+  // population-0 row (the face-state table's source without its x shift; at a
+  // no-slip face the cell's own row of opp(I)), and the no-slip bits
+  __shared__ long long s_row[16 * Q];
   __shared__ unsigned s_bb[16];
-  E *ring = reinterpret_cast<E *>(lines_smem);
-  const size_t stage_elems = (size_t)Q * la.window;
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nx = a.L.nx, ny = a.L.ny;
-  for (int k = tid; k < 16 * Q; k += LINES_THREADS) s_off[k] = a.face_off[k];
+  constexpr int NCW = LINES_THREADS / 32;  // consumer warps
+  for (int k = tid; k < 16 * Q; k += blockDim.x) {
+    const int fs = k / Q, I = k % Q;
+    const unsigned bb = a.face_bb[fs];
+    long long row = 0;
+    if (I > 0)
+      row = ((bb >> I) & 1u) ? (long long)L::opp(I) * a.L.S
+                             : a.face_off[k] + (long long)L::ex(I);  // undo the table's x shift
+    s_row[k] = row;
+  }
   if (tid < 16) s_bb[tid] = a.face_bb[tid];
   if (tid == 0) {
-    for (int s = 0; s < la.stages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < la.stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NCW);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     failed = 0;
   }
   __syncthreads();
-  // prologue: the first stages - 1 lines of this block
-  if (tid == 0)
-    for (int s = 0; s < la.stages - 1; ++s) {
-      const long long ln = blockIdx.x + (long long)s * gridDim.x;
-      if (ln < la.lines)
-        lines_issue<Q, E>(a, la, ln, ring + s * stage_elems, &bars[s], s_off, s_bb);
-    }
-  // thread 0's bookkeeping for a clean exit after a failed wait: the stages
-  // with copies in flight
-  unsigned inflight = 0u;
-  if (tid == 0)
-    for (int k = 0; k < la.stages - 1; ++k)
-      if (blockIdx.x + (long long)k * gridDim.x < la.lines) inflight |= 1u << k;
-  int s = 0;
-  unsigned pbits = 0u;  // bit k: parity of the next wait on stage k (thread 0)
-  // One thread waits for a stage's copies; the block meets it at one barrier
-  // per line, so no other warp spends issue slots polling the mbarrier.
-  if (tid == 0 && blockIdx.x < la.lines) {
-    if (mbar_wait_bounded(&bars[0], 0u)) {
-      inflight &= ~1u;
-      pbits ^= 1u;
-    } else {
-      failed = 1;
-    }
-  }
-  __syncthreads();
-  for (long long ln = blockIdx.x; ln < la.lines && !failed; ln += gridDim.x) {
-    // refill the stage the previous line used with the line stages - 1 ahead
-    // (every thread passed the barrier after finishing that line)
-    if (tid == 0) {
-      const long long nl = ln + (long long)(la.stages - 1) * gridDim.x;
-      const int ns = (s + la.stages - 1) % la.stages;
-      if (nl < la.lines) {
-        lines_issue<Q, E>(a, la, nl, ring + ns * stage_elems, &bars[ns], s_off, s_bb);
-        inflight |= 1u << ns;
+
+  if (warp == NCW) {  // ---- producer ---------------------------------------
+    int s = 0;
+    unsigned epar = 0u;  // bit k: parity of the next empty-wait on stage k
+    long long k = 0;
+    for (long long ln = blockIdx.x; ln < la.lines; ln += gridDim.x, ++k) {
+      if (k >= la.stages) {  // stage s is reused: every consumer warp released it
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait_bounded(&empty[s], (epar >> s) & 1u);
+        __syncwarp();
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok || failed) {
+          if (lane == 0) failed = 1;
+          break;
+        }
+        epar ^= 1u << s;
       }
+      lines_produce<Q, E>(a, la, ln, lines_smem + (size_t)s * la.stage_bytes, &full[s], s_row);
+      s = s + 1 == la.stages ? 0 : s + 1;
     }
-    const E *buf = ring + s * stage_elems;
+    // Leave no copy in flight: wait (bounded) for every stage's last batch.
+    if (lane == 0) {
+      const long long issued = k;
+      for (int q = 0; q < la.stages && q < issued; ++q) {
+        const long long last = q + ((issued - 1 - q) / la.stages) * la.stages;  // batch index
+        (void)mbar_wait_bounded(&full[q], (unsigned)((last / la.stages) & 1));
+      }
+      if (failed) atomicExch(la.err, LINES_TIMEOUT);
+    }
+    return;
+  }
+
+  // ---- consumers ----------------------------------------------------------
+  int s = 0;
+  unsigned fpar = 0u;  // bit k: parity of the next full-wait on stage k
+  for (long long ln = blockIdx.x; ln < la.lines; ln += gridDim.x) {
+    bool ok = true;
+    if (lane == 0) ok = mbar_wait_bounded(&full[s], (fpar >> s) & 1u);
+    __syncwarp();  // orders the stage's data, seen by lane 0's wait, before the warp's reads
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok || failed) {
+      if (lane == 0) failed = 1;
+      break;
+    }
+    fpar ^= 1u << s;
+    const unsigned char *st = lines_smem + (size_t)s * la.stage_bytes;
+    const E *buf = reinterpret_cast<const E *>(st);
+    const uint32_t *slinks =
+        reinterpret_cast<const uint32_t *>(st + (size_t)Q * la.window * sizeof(E));
+    const int *stiles = reinterpret_cast<const int *>(slinks + (size_t)la.nxw_pad * 32);
     const int y = (int)(ln % ny), z = (int)(ln / ny);
-    const int st = face_state(y, z, ny, a.L.nz);
-    const unsigned wbb = s_bb[st];
+    const int fst = face_state(y, z, ny, a.L.nz);
+    const unsigned wbb = s_bb[fst];
     const long long rowc = a.L.idx(0, y, z);  // cell x = 0, population 0
     for (int xb = 0; xb < nx; xb += LINES_CELLS) {
       // warp w takes the tiles 2w and 2w + 1 of this 512-cell block: cells x0
-      // and x0 + 32, the pairs of the register-fed kernel (same rounding keys)
-      const int x0 = xb + 64 * (tid >> 5) + lane, x1 = x0 + 32;
-      if (xb + 64 * (tid >> 5) >= nx) continue;  // warp entirely past the line
+      // and x0 + 32, the pairs of the register-fed kernel
+      const int x0 = xb + 64 * warp + lane, x1 = x0 + 32;
+      if (xb + 64 * warp >= nx) continue;  // warp entirely past the line
       const bool st0 = x0 < nx, st1 = x1 < nx;
-      // listed tiles of the warp's two 32-cell tiles (solid cells or links)
-      const long long trow = ((long long)z * ny + y) * a.nxw;
-      const int t0 = a.tile_index[trow + (x0 >> 5)];  // the warp's tile exists
-      const int t1 = st1 ? a.tile_index[trow + (x1 >> 5)] : -1;
-      const unsigned l0 = t0 >= 0 ? a.links_bits[(long long)t0 * SWEEP_BX + lane] : 0u;
-      const unsigned l1 = t1 >= 0 ? a.links_bits[(long long)t1 * SWEEP_BX + lane] : 0u;
+      const int w0 = x0 >> 5;
+      const unsigned l0 = stiles[w0] >= 0 ? slinks[w0 * 32 + lane] : 0u;
+      const unsigned l1 = (st1 && stiles[w0 + 1] >= 0) ? slinks[(w0 + 1) * 32 + lane] : 0u;
       const bool linked = __any_sync(0xffffffffu, ((l0 | l1) & 0x7FFFFFFFu) != 0u);
       float2 f[Q];
       static_for(
@@ -230,27 +282,11 @@ __global__ void __launch_bounds__(LINES_THREADS, MINB)
       for (int i = 0; i < Q; ++i)
         PairCodec<ST>::template put2<Q>(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i],
                                         a.L.fbase[i], st0, st1,
-                                        (unsigned)((ln * nx + x0) * Q + i));
+                                        (unsigned)((ln * nx + x0) * Q + i), a.f16_sr);
     }
-    // the next line's stage: thread 0 waits for its copies, then the barrier
-    // (which also orders every read of stage s before its refill)
-    const int s1 = s + 1 == la.stages ? 0 : s + 1;
-    if (tid == 0 && ln + gridDim.x < la.lines) {
-      if (mbar_wait_bounded(&bars[s1], (pbits >> s1) & 1u)) {
-        inflight &= ~(1u << s1);
-        pbits ^= 1u << s1;
-      } else {
-        failed = 1;
-      }
-    }
-    __syncthreads();
-    s = s1;
-  }
-  if (failed && tid == 0) {
-    atomicExch(la.err, LINES_TIMEOUT);
-    // let the copies this block issued land before its shared memory is released
-    for (int k = 0; k < la.stages; ++k)
-      if ((inflight >> k) & 1u) (void)mbar_wait_bounded(&bars[k], (pbits >> k) & 1u);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    s = s + 1 == la.stages ? 0 : s + 1;
   }
 }
 

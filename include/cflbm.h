@@ -68,6 +68,10 @@ enum cflbm_geom { CFLBM_GEOM_NONE = 0, CFLBM_GEOM_CYLINDER = 1, CFLBM_GEOM_SPHER
  *  SOA:  f[i][z][y][x] -- one array per population;
  *  ROWS: f[z][y][i][x] -- the Q rows of a (y, z) line are adjacent. */
 enum cflbm_layout { CFLBM_LAYOUT_SOA = 0, CFLBM_LAYOUT_ROWS = 1 };
+/* Rounding of FP16-deviation stores: to nearest, or stochastic (hardware
+ * cvt.rs fed with a hash of value and element: deterministic and identical
+ * across kernels and layouts). */
+enum cflbm_rounding { CFLBM_ROUND_NEAREST = 0, CFLBM_ROUND_STOCHASTIC = 1 };
 
 typedef struct cflbm_handle cflbm_handle;
 
@@ -93,6 +97,7 @@ typedef struct cflbm_config {
   int force_history;    /* capacity (steps) of the on-device force history; 0 = 65536 */
   int device;           /* CUDA device ordinal */
   int layout;           /* enum cflbm_layout */
+  int rounding;         /* enum cflbm_rounding (FP16 storage only) */
 } cflbm_config;
 
 /* Geometry/step counters and device layout of a handle. */
@@ -111,7 +116,8 @@ typedef struct cflbm_info {
 } cflbm_info;
 
 /* Defaults: D2Q9 64x32, FP64 storage and arithmetic, CHANNEL, free-slip y,
- * periodic z, tau0 = 0.03, u0 = 0.05, no body, no perturbation, ROWS layout. */
+ * periodic z, tau0 = 0.03, u0 = 0.05, no body, no perturbation, ROWS layout,
+ * round-to-nearest FP16 stores. */
 int cflbm_config_default(cflbm_config *cfg);
 
 /* Allocate device state and initialise it (f = equilibrium of the initial

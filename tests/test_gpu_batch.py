@@ -13,7 +13,7 @@ from cflbm import Batch, Solver
 pytestmark = pytest.mark.gpu
 
 
-def configs(storage="fp32"):
+def configs(storage="fp32", rounding="nearest"):
     rng = np.random.default_rng(5)
     out = []
     for k in range(3):
@@ -23,7 +23,8 @@ def configs(storage="fp32"):
         re = float(rng.uniform(40, 200))
         out.append(dict(lattice=9, nx=nx, ny=ny, tau0=3 * 0.05 * d / re, u0=0.05,
                         wall_y="freeslip", geom="cylinder", cx=nx / 4, cy=ny / 2, diam=d,
-                        perturb_amp=1e-3, seed=100 + k, storage=storage, compute="fp32"))
+                        perturb_amp=1e-3, seed=100 + k, storage=storage, compute="fp32",
+                        rounding=rounding))
     return out
 
 
@@ -33,9 +34,9 @@ def alone(cfg, steps):
         return s.get_f(), s.force_history(), s.macros()[0]
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16dev"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16dev", "fp16dev-sr"])
 def test_batch_instances_match_standalone_channels(cuda, storage):
-    cfgs = configs(storage)
+    cfgs = configs(storage.split("-")[0], "stochastic" if storage.endswith("-sr") else "nearest")
     steps = 23
     with Batch(cfgs, graph_steps=6, autotune=True) as b:
         info = b.info()

@@ -94,7 +94,10 @@ def test_ref2ds_matches_oracle_longer_run(cuda, compute, tol):
     sl = (slice(2, 2 + nx), slice(2, 2 + ny))
     assert rel_err(u[0], o["u"][sl].T) < tol
     assert rel_err(v[0], o["v"][sl].T) < tol
-    assert rel_err(p[0], o["p"][sl].T) < tol
+    # p is the deviation of sum(f)/3 from rest, ~4e-3 here: its error is bounded
+    # on the scale of the pressure itself (1/3), which FP32 rounds at ~2e-8
+    # per step, not on the deviation's own small maximum
+    assert np.max(np.abs(p[0] - o["p"][sl].T)) < tol * (1.0 / 3.0)
 
 
 def test_ref2d_matches_oracle_longer_run(cuda):
@@ -291,14 +294,17 @@ def test_steps_are_deterministic_and_resumable(cuda):
 
 
 @pytest.mark.parametrize("name", ["d2q9_cyl_freeslip", "d3q27_cyl", "d3q27_noslip"])
-@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16dev"])
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16dev", "fp16dev-sr"])
 def test_layouts_give_identical_states(cuda, name, storage):
+    """Every kernel (register-fed pairs, line-staged rows, one-cell listed
+    tiles) rounds a state alike, FP16 stochastic rounding included."""
     case = CHANNEL_CASES[name]
     steps = 60 if case["lattice"] == 9 else 12
+    rounding = "stochastic" if storage.endswith("-sr") else "nearest"
     out = []
     for layout in ("soa", "rows"):
-        with Solver(perturb_amp=1e-3, layout=layout, storage=storage, compute="fp32",
-                    **case) as s:
+        with Solver(perturb_amp=1e-3, layout=layout, storage=storage.split("-")[0],
+                    compute="fp32", rounding=rounding, **case) as s:
             s.step(steps)
             out.append((s.get_f(), s.force_history()))
     assert np.array_equal(out[0][0], out[1][0])
