@@ -67,9 +67,10 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-launch DRAM bytes of the sweep from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "sweep_d3q27_512x128x128.md")
+def profile_traffic(name="sweep_fp64_d3q27_512x128x128.md"):
+    """Per-launch DRAM bytes of the headline sweep (FP64 storage and arithmetic)
+    from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -187,7 +188,7 @@ def form_errors(s, oracle_run):
 
 
 def variant(cflbm, local, storage, compute, layout, steps, warmup, oracle_run,
-            rounding="nearest"):
+            rounding="stochastic"):
     import torch
     with cflbm.Solver(device=local, storage=storage, compute=compute, layout=layout,
                       rounding=rounding, **WORKLOAD) as s:
@@ -267,9 +268,9 @@ def run_gb300(args):
                                   ("fp32_store_soa", "fp32", "fp32", "soa"),
                                   ("fp16dev_store", "fp16dev", "fp32", "rows"),
                                   ("fp16dev_store_soa", "fp16dev", "fp32", "soa"),
-                                  ("fp16dev_sr_store_soa", "fp16dev", "fp32", "soa")):
+                                  ("fp16dev_rn_store_soa", "fp16dev", "fp32", "soa")):
             v = variant(cflbm, local, st, cp, lay, steps, min(warmup, 5), oracle_run,
-                        "stochastic" if "_sr_" in name else "nearest")
+                        "nearest" if "_rn_" in name else "stochastic")
             v["hbm_frac"] = v["bytes_per_cell"] * CELLS / (v["sweep_us"] * 1e-6) / 1e9 / peak
             extra[name] = {k: (round(x, 4) if isinstance(x, float) else x) for k, x in v.items()}
 
@@ -371,9 +372,9 @@ def run_channel2d(args):
         for name, st, cp in (("fp64", "fp64", "fp64"), ("df64", "fp64", "df64"),
                              ("fp64_store", "fp64", "fp32"), ("fp32_store", "fp32", "fp32"),
                              ("fp16dev_store", "fp16dev", "fp32"),
-                             ("fp16dev_sr_store", "fp16dev", "fp32")):
+                             ("fp16dev_rn_store", "fp16dev", "fp32")):
             with cflbm.Solver(device=local, storage=st, compute=cp, force_history=steps + 8,
-                              rounding="stochastic" if "_sr_" in name else "nearest",
+                              rounding="nearest" if "_rn_" in name else "stochastic",
                               **CH2D) as s:
                 stream = torch.cuda.ExternalStream(s.stream_ptr())
                 f0 = s.get_f()
@@ -556,22 +557,24 @@ def run_profile(args):
     else:
         wl = dict(WORKLOAD, nx=args.nx, ny=args.ny, nz=args.nz, cx=args.nx / 4.0,
                   cy=args.ny / 2.0)
-    with cflbm.Solver(storage=args.storage, compute=args.compute, layout=args.layout,
-                      **wl) as s:
-        s.step(args.warmup)
-        s.synchronize()
-        t0 = time.perf_counter()
-        s.step(args.steps)
-        s.synchronize()
-        dt = time.perf_counter() - t0
-        info = s.info()
-    cells = args.nx * args.ny * args.nz
-    print(json.dumps({"profile_case": [args.nx, args.ny, args.nz],
-                      "profile": "ref3d" if args.ref else "channel", "storage": args.storage,
-                      "compute": args.compute, "steps": args.steps,
-                      "mlups_wall": cells * args.steps / dt / 1e6,
-                      "bytes_per_cell": info.bytes_per_cell_step,
-                      "device_bytes": info.device_bytes}))
+    for layout in args.layout.split(","):  # one layout after the other
+        with cflbm.Solver(storage=args.storage, compute=args.compute, layout=layout,
+                          rounding=args.rounding, **wl) as s:
+            s.step(args.warmup)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(args.steps)
+            s.synchronize()
+            dt = time.perf_counter() - t0
+            info = s.info()
+        cells = args.nx * args.ny * args.nz
+        print(json.dumps({"profile_case": [args.nx, args.ny, args.nz],
+                          "profile": "ref3d" if args.ref else "channel",
+                          "storage": args.storage, "compute": args.compute, "layout": layout,
+                          "rounding": args.rounding, "steps": args.steps,
+                          "mlups_wall": cells * args.steps / dt / 1e6,
+                          "bytes_per_cell": info.bytes_per_cell_step,
+                          "device_bytes": info.device_bytes}))
     return 0
 
 
@@ -598,7 +601,10 @@ def main():
     ap.add_argument("--nz", type=int, default=NZ)
     ap.add_argument("--storage", default="fp64", choices=["fp64", "fp32", "fp16dev"])
     ap.add_argument("--compute", default="fp32", choices=["fp64", "fp32", "df64"])
-    ap.add_argument("--layout", default="rows", choices=["soa", "rows"])
+    ap.add_argument("--layout", default="rows",
+                    help="soa or rows; with --profile a comma list runs each in turn")
+    ap.add_argument("--rounding", default="stochastic", choices=["nearest", "stochastic"],
+                    help="FP16 storage rounding (with --profile)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 20000 if args.workload == "channel2d" else 1000

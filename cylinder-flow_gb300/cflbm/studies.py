@@ -21,7 +21,8 @@ adjoint_study: the differentiation problem (D2Q9 1024x256 channel, cylinder
 D=32 at (200, 128), porosity on a 128x128 box, mean drag over steps 5000-7000
 of 7000, checkpoints every 100).  Runs the FP32 and FP64 adjoints, compares
 them, and checks the FP64 gradient against central differences (h = 1e-4) of
-the FP64 solver for u_in, tau and 16 seeded porosity directions.
+the FP64 solver for u_in, tau and 16 seeded porosity directions; along each
+direction also at 2h, and the Richardson extrapolation of the two.
 
     python -m cflbm.studies adjoint --out adjoint.json
 
@@ -29,8 +30,9 @@ batch_study: the batched form (64 D2Q9 cylinder channels, widths 256-1024 and
 heights 64-256 in multiples of 32, D in [8, 32], Re in [40, 200], u_in = 0.05,
 FP32 storage, 20000 steps in one launch per step over all channels, replayed
 from a 100-step CUDA graph, autotuned launch shape) against the same channels run one
-at a time with FP64 storage and arithmetic; per-instance Cd error against that
-FP64 run.
+at a time with FP32 storage and arithmetic (the gain from batching alone) and
+with FP64 storage and arithmetic (the plain drop-in); per-instance Cd error
+against that FP64 run.
 
     python -m cflbm.studies batch --out batch.json
 """
@@ -62,8 +64,8 @@ FORMS = [  # name, storage, compute, FP16 rounding
     ("df64_arith", "fp64", "df64", "nearest"),
     ("fp64_store", "fp64", "fp32", "nearest"),
     ("fp32_store", "fp32", "fp32", "nearest"),
-    ("fp16dev_store", "fp16dev", "fp32", "nearest"),
-    ("fp16dev_sr_store", "fp16dev", "fp32", "stochastic"),
+    ("fp16dev_store", "fp16dev", "fp32", "stochastic"),
+    ("fp16dev_rn_store", "fp16dev", "fp32", "nearest"),
 ]
 
 
@@ -215,14 +217,29 @@ def adjoint_study(steps=7000, window=(5000, 7000), checkpoint_every=100, box=128
     for k in range(directions):
         d = rng.standard_normal(alpha.shape) * mask
         d /= np.max(np.abs(d))
-        ap = (alpha + h * d).astype(np.float32).astype(np.float64)
-        am = (alpha - h * d).astype(np.float32).astype(np.float64)
-        f = J(ap, u_in, tau) - J(am, u_in, tau)
-        a64 = float(np.sum(g64["dJ_dalpha"] * (ap - am)))
-        a32 = float(np.sum(g32["dJ_dalpha"] * (ap - am)))
-        dirs.append({"fd": f, "adjoint_fp64": a64, "adjoint_fp32": a32,
-                     "rel_err_fp64": abs(a64 - f) / abs(f), "rel_err_fp32": abs(a32 - f) / abs(f)})
+        # central differences at h and 2h along d, each divided by its own
+        # (FP32-rounded) step so they estimate the same derivative dJ/dalpha . d;
+        # Richardson's (4 D(h) - D(2h)) / 3 removes their h^2 truncation term
+        dd = []
+        for hk in (h, 2 * h):
+            ap = (alpha + hk * d).astype(np.float32).astype(np.float64)
+            am = (alpha - hk * d).astype(np.float32).astype(np.float64)
+            step = ap - am
+            dd.append(((J(ap, u_in, tau) - J(am, u_in, tau)) / (2 * hk),
+                       float(np.sum(g64["dJ_dalpha"] * step)) / (2 * hk),
+                       float(np.sum(g32["dJ_dalpha"] * step)) / (2 * hk)))
+        (f1, a64, a32), (f2, a64b, _) = dd
+        # the Richardson combination of the adjoint projections (the FP32 rounding
+        # of the two steps differs slightly) against that of the differences
+        fr = (4 * f1 - f2) / 3
+        ar = (4 * a64 - a64b) / 3
+        dirs.append({"fd_h": f1, "fd_2h": f2, "fd_richardson": fr, "adjoint_fp64": a64,
+                     "adjoint_fp32": a32,
+                     "rel_err_fp64_h": abs(a64 - f1) / abs(f1),
+                     "rel_err_fp64": abs(ar - fr) / abs(fr),
+                     "rel_err_fp32": abs(a32 - f1) / abs(f1)})
     fd["directions"] = dirs
+    fd["max_rel_err_fp64_h"] = max(d["rel_err_fp64_h"] for d in dirs)
     fd["max_rel_err_fp64"] = max(d["rel_err_fp64"] for d in dirs)
     fd["median_rel_err_fp64"] = float(np.median([d["rel_err_fp64"] for d in dirs]))
     fd["max_rel_err_fp32"] = max(d["rel_err_fp32"] for d in dirs)
@@ -291,21 +308,31 @@ def batch_study(n=64, steps=20000, graph_steps=100, window=10000, peak_gbs=None,
             json.dump(res, fh, indent=1)
     if not sequential:
         return res
-    seq_wall = 0.0
-    cd64 = []
-    for k, c in enumerate(cfgs):
-        with Solver(**c, storage="fp64", compute="fp64", force_history=steps + 8) as s:
-            s.synchronize()
-            t = time.perf_counter()
-            s.step(steps)
-            s.synchronize()
-            seq_wall += time.perf_counter() - t
-            hist = s.force_history(steps)
-        cd64.append(analysis.summary(hist, c["u0"], c["diam"], c["diam"], window)["cd_mean"])
+    def sequential(storage, compute):
+        """The same channels one at a time (each its own graph-replayed step
+        loop), and each one's mean drag over the window."""
+        wall, cds = 0.0, []
+        for c in cfgs:
+            with Solver(**c, storage=storage, compute=compute, force_history=steps + 8) as s:
+                s.synchronize()
+                t = time.perf_counter()
+                s.step(steps)
+                s.synchronize()
+                wall += time.perf_counter() - t
+                hist = s.force_history(steps)
+                b = s.info().bytes_per_cell_step
+            cds.append(analysis.summary(hist, c["u0"], c["diam"], c["diam"], window)["cd_mean"])
+        return {"wall_s": wall, "mlups": cells * steps / wall / 1e6,
+                "hbm_frac": b * cells * steps / wall / 1e9 / peak_gbs}, cds
+
+    # the gain from batching alone: the same FP32 storage and arithmetic, one
+    # channel at a time; then the plain FP64 drop-in, the Cd reference
+    res["sequential_fp32"], cd32s = sequential("fp32", "fp32")
+    res["speedup_vs_fp32_sequential"] = res["batch"]["mlups"] / res["sequential_fp32"]["mlups"]
+    res["cd_fp32_batch_vs_sequential_max_abs"] = max(abs(a - b) for a, b in zip(cd32, cd32s))
+    print("sequential_fp32", json.dumps(res["sequential_fp32"]), flush=True)
+    res["sequential_fp64"], cd64 = sequential("fp64", "fp64")
     err = [abs(a - b) / abs(b) for a, b in zip(cd32, cd64)]
-    res["sequential_fp64"] = {
-        "wall_s": seq_wall, "mlups": cells * steps / seq_wall / 1e6,
-        "hbm_frac": 144.0 * cells * steps / seq_wall / 1e9 / peak_gbs}
     res["speedup"] = res["batch"]["mlups"] / res["sequential_fp64"]["mlups"]
     res["cd"] = {"fp32_batch": cd32, "fp64_sequential": cd64, "rel_err": err,
                  "max_rel_err": max(err), "median_rel_err": float(np.median(err))}

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -265,7 +266,7 @@ int cflbm_config_default(cflbm_config *c) {
   c->geom = CFLBM_GEOM_NONE;
   c->seed = 1234;
   c->layout = CFLBM_LAYOUT_ROWS;
-  c->rounding = CFLBM_ROUND_NEAREST;
+  c->rounding = CFLBM_ROUND_STOCHASTIC;
   return CFLBM_OK;
 }
 
@@ -476,7 +477,11 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   if ((rc = dev_alloc_t(h, &h->d_sums, 4))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_err, 1))) return rc;
   CK_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream));
+  // FP16 ROWS channel sweeps: the line-staged kernel unless the environment
+  // variable CFLBM_FP16_SWEEP says "registers" (the register-fed pair kernel)
+  const char *fp16_sweep = std::getenv("CFLBM_FP16_SWEEP");
   h->lines = cfg->profile == CFLBM_PROFILE_CHANNEL &&
+             !(fp16_sweep && std::strcmp(fp16_sweep, "registers") == 0) &&
              lines_supported(Q, cfg->storage, cfg->layout == CFLBM_LAYOUT_ROWS,
                              cfg->alpha != nullptr, nx);
   if (h->lines) CK_CUDA(lines_prepare());
@@ -617,6 +622,18 @@ void set_relax(SweepArgs &a, int Q, int, double omega) {
   }
 }
 
+void set_offsets(SweepArgs &a, int Q) {
+  for (int i = 0; i < 27; ++i) {
+    a.doff[i] = a.poff[i] = 0;
+    if (i >= Q) continue;
+    const int ex = Q == 27 ? Lat<27>::ex(i) : Lat<9>::ex(i);
+    const int ey = Q == 27 ? Lat<27>::ey(i) : Lat<9>::ey(i);
+    const int ez = Q == 27 ? Lat<27>::ez(i) : 0;
+    a.doff[i] = (long long)i * a.L.S;
+    a.poff[i] = a.doff[i] - a.L.off(ex, ey, ez);
+  }
+}
+
 // Arguments of the channel sweep of handle h reading fa and writing fb.
 SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool write_macros) {
   SweepArgs sa{};
@@ -626,6 +643,7 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   sa.mask = h->d_mask;
   sa.nxw = h->nxw;
   set_relax(sa, h->Q, h->cfg.storage, h->omega);
+  set_offsets(sa, h->Q);
   sa.f16_sr = h->cfg.rounding == CFLBM_ROUND_STOCHASTIC;
   sa.alpha = h->d_alpha;
   if (write_macros) {
@@ -742,6 +760,7 @@ static int one_step(cflbm_handle *h, bool write_macros) {
   sa.mask = h->d_mask;
   sa.nxw = h->nxw;
   set_relax(sa, Q, st, h->omega);
+  set_offsets(sa, Q);
   sa.f16_sr = h->cfg.rounding == CFLBM_ROUND_STOCHASTIC;
   sa.ref_override = ref ? 1 : 0;
   sa.inlet_u = h->d_inlet;

@@ -209,17 +209,19 @@ template <> struct Store<float> {
 // 2^12 keeps every value above 2^-24/2^12 normal down to 1.5e-8 with room to
 // spare.  Decode: one FMA (the product by 2^-12 is exact).
 //
-// Encode (the sweeps' stores): round to nearest (default), or stochastically
-// (cflbm_config::rounding) with sm_100-family hardware stochastic rounding,
+// Encode (the sweeps' stores): round stochastically (default), or to nearest
+// (cflbm_config::rounding); stochastic with sm_100-family hardware rounding,
 // cvt.rs.f16x2.f32, fed with a hash of the value's FP32 bits and its element
 // (key = cell * Q + i): runs stay deterministic, repeat and resume exactly, and
 // every kernel and layout rounds a state alike.  cvt.rs rounds the upper half
 // of its result with rbits[28:16] and the lower half with rbits[12:0], so a
 // pair store gives each value the bits [28:16] of its own hash (byte_perm
 // 0x3276 below) and a single store the same bits of the same hash.
-// Measured on the D2Q9 400x100 cylinder channel (drag averaged over whole
-// shedding periods, steps 30,000-40,000, three perturbation seeds, against
-// FP64): nearest 4.6e-4 .. 6.5e-4, stochastic 6e-5 .. 1.1e-3.
+// Drag error against FP64 arithmetic: D3Q27 768x384x384 sphere, Re 300, mean
+// over steps 15,000-20,000: stochastic 1.3e-4, nearest 1.04e-3 (the steady
+// part of round-to-nearest's error adds up over the run); D2Q9 400x100
+// cylinder, periodic state, three perturbation seeds: stochastic 1.5e-4 ..
+// 8.6e-4, nearest 4.6e-4 .. 6.5e-4.
 constexpr float F16_SCALE = 4096.0f;
 __device__ __forceinline__ unsigned f16_hash(float sv, unsigned key) {
   return (__float_as_uint(sv) ^ (key * 0x9E3779B1u)) * 0x85EBCA77u;

@@ -70,6 +70,11 @@ struct SweepArgs {
   float rkf[RK_N];
   float rkl[RK_N];
   bool f16_sr;           // FP16 storage: stochastic rounding of stores (else nearest)
+  // Per direction I, in elements: doff = I * S (the population's storage
+  // offset) and poff = doff - L.off(e_I) (the plain pull's source), kernel
+  // parameters so that no thread forms them with 64-bit products.
+  long long doff[27];
+  long long poff[27];
   int ref_override;      // reference profiles: inlet u at x = 0, p = 0 at x = nx-1
   const double *inlet_u; // ny*nz inlet velocity profile (reference profiles)
   const float *alpha;    // nx*ny*nz Brinkman porosity or null
@@ -187,6 +192,8 @@ cudaError_t launch_fill_value(int Q, int store, const Layout &L, void *f, cudaSt
 // lattice Q (any storage kind `store`: the codecs hand the arithmetic the
 // populations themselves).
 void set_relax(SweepArgs &a, int Q, int store, double omega);
+// Fill doff/poff of a sweep from its layout a.L.
+void set_offsets(SweepArgs &a, int Q);
 
 // Line-staged sweep (lines.cu): whether it covers a handle's form, its one-time
 // set-up (shared-memory opt-in) and its launch.

@@ -619,7 +619,7 @@ __device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restric
                                        bool act1, bool inlet0, const SweepArgs &a) {
   using Dd = DirC<Q, I>;
   using PC = PairCodec<ST>;
-  const long long off = I * S - (Dd::ex + Dd::ey * rs + Dd::ez * zs);
+  const long long off = a.poff[I];
   float r0 = 0.0f, r1 = 0.0f;
   if constexpr (Dd::ex < 0) {  // the outlet column repeats itself (pm = p - 1 there)
     if (act0) r0 = PC::raw(__ldg(pm0 + off));
@@ -658,8 +658,8 @@ __device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__
     constexpr long long OS = Dd::opp;
     const float b0 = bb0 ? a.L.fbase[Dd::opp] : a.L.fbase[I];
     const float b1 = bb1 ? a.L.fbase[Dd::opp] : a.L.fbase[I];
-    const float r0 = PC::raw(__ldg(p + (bb0 ? OS * S : s0)));
-    const float r1 = act1 ? PC::raw(__ldg(p + (bb1 ? OS * S + 32 : s1))) : 0.0f;
+    const float r0 = PC::raw(__ldg(p + (bb0 ? a.doff[OS] : s0)));
+    const float r1 = act1 ? PC::raw(__ldg(p + (bb1 ? a.doff[OS] + 32 : s1))) : 0.0f;
     float2 v = PC::dec(make_float2(r0, r1), make_float2(b0, b1));
     if constexpr (Dd::ex > 0) v.x = (!bb0 && inlet0) ? a.f_in_f[I] : v.x;
     return v;

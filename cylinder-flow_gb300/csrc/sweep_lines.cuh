@@ -137,6 +137,67 @@ __device__ __forceinline__ void lines_produce(const SweepArgs &a, const LinesArg
   }
 }
 
+// Cells x0 and x0 + 32 of a staged line: pulls from the stage's rows (rows
+// already chosen per face state by the producer), the per-cell x rules (inlet
+// equilibrium at x = 0, zero gradient at x = nx - 1), and -- NOSLIP: the line
+// lies on a no-slip face (wbb: its bounced directions, unshifted and decoded
+// with the opposite's base); LINKED: a cell of the pair has solid links (their
+// bounced populations from global memory; solid cells get p = u = 0).  The
+// arithmetic is channel2_cells', so the states are bit-identical to the
+// register-fed kernel's.
+template <int Q, class ST, bool NOSLIP, bool LINKED>
+__device__ __forceinline__ void lines_pair(const SweepArgs &a, const typename Store<ST>::elem *buf,
+                                           int window, unsigned wbb, long long rowc, int x0,
+                                           unsigned l0, unsigned l1, long long key) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx;
+  const int x1 = x0 + 32;
+  const bool st0 = x0 < nx, st1 = x1 < nx;
+  float2 f[Q];
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        constexpr int ex = L::ex(I);
+        const bool bbI = NOSLIP && ((wbb >> I) & 1u);
+        const int sx = bbI ? 0 : ex;
+        const E *row = buf + (size_t)I * window + 8;  // row[x'] = element of x'
+        int xs0 = x0 - sx, xs1 = x1 - sx;
+        if constexpr (ex < 0) {  // zero gradient: the outlet column repeats itself
+          xs0 = (x0 == nx - 1 && !bbI) ? x0 : xs0;
+          xs1 = (x1 == nx - 1 && !bbI) ? x1 : xs1;
+        }
+        const float b = bbI ? a.L.fbase[L::opp(I)] : a.L.fbase[I];
+        const float r0 = st0 ? PairCodec<ST>::raw(row[xs0]) : 0.0f;
+        const float r1 = st1 ? PairCodec<ST>::raw(row[xs1]) : 0.0f;
+        float2 v = PairCodec<ST>::dec(make_float2(r0, r1), make_float2(b, b));
+        if constexpr (ex > 0) v.x = (x0 == 0 && !bbI) ? a.f_in_f[I] : v.x;
+        if constexpr (LINKED && I > 0) {  // bounce-back off solid sources
+          const E *fa = static_cast<const E *>(a.fa);
+          const long long ob = a.doff[L::opp(I)] + rowc;
+          if ((l0 >> I) & 1u)
+            v.x = SF::template load<float, L>(fa + ob + x0, a.L.fbase[L::opp(I)]);
+          if ((l1 >> I) & 1u)
+            v.y = SF::template load<float, L>(fa + ob + x1, a.L.fbase[L::opp(I)]);
+        }
+        f[I] = v;
+      },
+      std::make_integer_sequence<int, Q>{});
+  float2 rho3, ux, uy, uz;
+  moments<L, float2, SF>(f, rho3, ux, uy, uz);
+  if constexpr (LINKED) {
+    if (l0 >> 31) { rho3.x = 0.0f; ux.x = 0.0f; uy.x = 0.0f; uz.x = 0.0f; }
+    if (l1 >> 31) { rho3.y = 0.0f; ux.y = 0.0f; uy.y = 0.0f; uz.y = 0.0f; }
+  }
+  bgk_relax_v<L, float2, SF>(f, rho3, ux, uy, uz, a);
+  E *__restrict__ q = static_cast<E *>(a.fb) + rowc;
+#pragma unroll
+  for (int i = 0; i < Q; ++i)
+    PairCodec<ST>::template put2<Q>(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i],
+                                    a.L.fbase[i], st0, st1, (unsigned)(key + i), a.f16_sr);
+}
+
 // Block: LINES_THREADS consumer threads (8 warps, two cells each per 512-cell
 // block of a line) and one producer warp.  Stage s is handed over with two
 // mbarriers: full[s] completes when the stage's copies have landed, empty[s]
@@ -237,52 +298,16 @@ __global__ void __launch_bounds__(LINES_THREADS + 32, MINB)
       // and x0 + 32, the pairs of the register-fed kernel
       const int x0 = xb + 64 * warp + lane, x1 = x0 + 32;
       if (xb + 64 * warp >= nx) continue;  // warp entirely past the line
-      const bool st0 = x0 < nx, st1 = x1 < nx;
       const int w0 = x0 >> 5;
       const unsigned l0 = stiles[w0] >= 0 ? slinks[w0 * 32 + lane] : 0u;
-      const unsigned l1 = (st1 && stiles[w0 + 1] >= 0) ? slinks[(w0 + 1) * 32 + lane] : 0u;
-      const bool linked = __any_sync(0xffffffffu, ((l0 | l1) & 0x7FFFFFFFu) != 0u);
-      float2 f[Q];
-      static_for(
-          [&](auto ic) {
-            constexpr int I = decltype(ic)::value;
-            constexpr int ex = L::ex(I);
-            const int sx = ((wbb >> I) & 1u) ? 0 : ex;
-            const E *row = buf + (size_t)I * la.window + 8;  // row[x'] = element of x'
-            int xs0 = x0 - sx, xs1 = x1 - sx;
-            if constexpr (ex < 0) {  // zero gradient: the outlet column repeats itself
-              xs0 = (x0 == nx - 1 && sx != 0) ? x0 : xs0;
-              xs1 = (x1 == nx - 1 && sx != 0) ? x1 : xs1;
-            }
-            const float b = ((wbb >> I) & 1u) ? a.L.fbase[L::opp(I)] : a.L.fbase[I];
-            const float r0 = st0 ? PairCodec<ST>::raw(row[xs0]) : 0.0f;
-            const float r1 = st1 ? PairCodec<ST>::raw(row[xs1]) : 0.0f;
-            float2 v = PairCodec<ST>::dec(make_float2(r0, r1), make_float2(b, b));
-            if constexpr (ex > 0) v.x = (x0 == 0 && sx != 0) ? a.f_in_f[I] : v.x;
-            if constexpr (I > 0) {
-              if (linked) {  // warp-uniform: bounce-back off solid sources
-                const E *fa = static_cast<const E *>(a.fa);
-                const long long ob = (long long)L::opp(I) * a.L.S + rowc;
-                if ((l0 >> I) & 1u)
-                  v.x = SF::template load<float, L>(fa + ob + x0, a.L.fbase[L::opp(I)]);
-                if ((l1 >> I) & 1u)
-                  v.y = SF::template load<float, L>(fa + ob + x1, a.L.fbase[L::opp(I)]);
-              }
-            }
-            f[I] = v;
-          },
-          std::make_integer_sequence<int, Q>{});
-      float2 rho3, ux, uy, uz;
-      moments<L, float2, SF>(f, rho3, ux, uy, uz);
-      if (l0 >> 31) { rho3.x = 0.0f; ux.x = 0.0f; uy.x = 0.0f; uz.x = 0.0f; }
-      if (l1 >> 31) { rho3.y = 0.0f; ux.y = 0.0f; uy.y = 0.0f; uz.y = 0.0f; }
-      bgk_relax_v<L, float2, SF>(f, rho3, ux, uy, uz, a);
-      E *__restrict__ q = static_cast<E *>(a.fb) + rowc;
-#pragma unroll
-      for (int i = 0; i < Q; ++i)
-        PairCodec<ST>::template put2<Q>(q + i * a.L.S + x0, q + i * a.L.S + x1, f[i],
-                                        a.L.fbase[i], st0, st1,
-                                        (unsigned)((ln * nx + x0) * Q + i), a.f16_sr);
+      const unsigned l1 = (x1 < nx && stiles[w0 + 1] >= 0) ? slinks[(w0 + 1) * 32 + lane] : 0u;
+      // solid links or solid cells in the pair
+      const bool linked = __any_sync(0xffffffffu, (l0 | l1) != 0u);
+      // warp-uniform: pairs off the no-slip faces (every line of the benchmark
+      // channels) without solid links or cells take the lean instantiation
+      const long long key = (ln * nx + x0) * Q;
+      if (wbb || linked) lines_pair<Q, ST, true, true>(a, buf, la.window, wbb, rowc, x0, l0, l1, key);
+      else lines_pair<Q, ST, false, false>(a, buf, la.window, 0u, rowc, x0, l0, l1, key);
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);

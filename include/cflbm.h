@@ -97,7 +97,7 @@ typedef struct cflbm_config {
   int force_history;    /* capacity (steps) of the on-device force history; 0 = 65536 */
   int device;           /* CUDA device ordinal */
   int layout;           /* enum cflbm_layout */
-  int rounding;         /* enum cflbm_rounding (FP16 storage only) */
+  int rounding;         /* enum cflbm_rounding (FP16 storage only; default stochastic) */
 } cflbm_config;
 
 /* Geometry/step counters and device layout of a handle. */
@@ -117,7 +117,7 @@ typedef struct cflbm_info {
 
 /* Defaults: D2Q9 64x32, FP64 storage and arithmetic, CHANNEL, free-slip y,
  * periodic z, tau0 = 0.03, u0 = 0.05, no body, no perturbation, ROWS layout,
- * round-to-nearest FP16 stores. */
+ * stochastic rounding of FP16 stores. */
 int cflbm_config_default(cflbm_config *cfg);
 
 /* Allocate device state and initialise it (f = equilibrium of the initial

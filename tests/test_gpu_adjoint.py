@@ -6,9 +6,10 @@ tau and the porosity field (along 16 seeded directions) are compared with
 central differences at h = 1e-4 of the FP64 GPU solver and of the CPU oracle,
 the FP32 adjoint with the FP64 one, and checkpoint spacings with each other.
 
-Tolerances: FP64 adjoint vs FP64 finite differences 1e-5 relative (the
-differences' truncation error at h = 1e-4 is ~1e-8); FP32 adjoint vs FP64
-adjoint 1e-2 relative (FP32 round-off accumulated over the run).
+Tolerances: FP64 adjoint vs FP64 finite differences 1e-5 relative for the
+scalars; 1e-4 relative (no absolute floor) along every porosity direction,
+against the Richardson extrapolation of differences at h and 2h; FP32 adjoint vs
+FP64 adjoint 1e-2 relative (FP32 round-off accumulated over the run).
 """
 from __future__ import annotations
 
@@ -84,6 +85,12 @@ def test_adjoint_scalars_match_finite_differences(cuda, wall):
 
 
 def test_adjoint_porosity_gradient_along_16_directions(cuda):
+    """Relative error of the projection dJ/dalpha . d along 16 seeded random
+    directions, each against central differences at h and 2h combined by
+    Richardson extrapolation, (4 D(h) - D(2h)) / 3, which removes the
+    differences' h^2 truncation term: a direction whose projection is small
+    next to J's third derivative along it would otherwise read that term as
+    adjoint error."""
     r = adj()
     g = r["dJ_dalpha"]
     a = alpha_field()
@@ -91,17 +98,20 @@ def test_adjoint_porosity_gradient_along_16_directions(cuda):
     rng = np.random.default_rng(2024)
     box = np.zeros_like(a)
     box[8:40, 14:46] = 1.0
-    worst = 0.0
+    errs = []
     for _ in range(16):
         d = rng.standard_normal(a.shape) * box
         d /= np.max(np.abs(d))
-        ap = (a + H * d).astype(np.float32).astype(np.float64)
-        am = (a - H * d).astype(np.float32).astype(np.float64)
-        fd = J_gpu(c, ap, U_IN, TAU) - J_gpu(c, am, U_IN, TAU)
-        ad = float(np.sum(g * (ap - am)))
-        scale = max(abs(ad), 1e-3 * np.linalg.norm(g) * np.linalg.norm(ap - am))
-        worst = max(worst, abs(fd - ad) / scale)
-    assert worst <= 1e-5, worst
+        fd, ad = [], []
+        for h in (H, 2 * H):
+            ap = (a + h * d).astype(np.float32).astype(np.float64)
+            am = (a - h * d).astype(np.float32).astype(np.float64)
+            fd.append((J_gpu(c, ap, U_IN, TAU) - J_gpu(c, am, U_IN, TAU)) / (2 * h))
+            ad.append(float(np.sum(g * (ap - am))) / (2 * h))
+        fr = (4 * fd[0] - fd[1]) / 3
+        ar = (4 * ad[0] - ad[1]) / 3
+        errs.append(abs(ar - fr) / abs(fr))
+    assert max(errs) <= 1e-4, errs
 
 
 def test_adjoint_matches_oracle_finite_differences(cuda):
