@@ -477,11 +477,12 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
   if ((rc = dev_alloc_t(h, &h->d_sums, 4))) return rc;
   if ((rc = dev_alloc_t(h, &h->d_err, 1))) return rc;
   CK_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream));
-  // FP16 ROWS channel sweeps: the line-staged kernel unless the environment
-  // variable CFLBM_FP16_SWEEP says "registers" (the register-fed pair kernel)
+  // FP16 ROWS channel sweeps: the register-fed pair kernel; the line-staged
+  // kernel (slower on GB300: 0.37 against 0.57 of the copy peak at 512x128x128)
+  // when the environment variable CFLBM_FP16_SWEEP says "lines"
   const char *fp16_sweep = std::getenv("CFLBM_FP16_SWEEP");
   h->lines = cfg->profile == CFLBM_PROFILE_CHANNEL &&
-             !(fp16_sweep && std::strcmp(fp16_sweep, "registers") == 0) &&
+             (fp16_sweep && std::strcmp(fp16_sweep, "lines") == 0) &&
              lines_supported(Q, cfg->storage, cfg->layout == CFLBM_LAYOUT_ROWS,
                              cfg->alpha != nullptr, nx);
   if (h->lines) CK_CUDA(lines_prepare());

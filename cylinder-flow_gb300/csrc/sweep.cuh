@@ -468,9 +468,19 @@ template <> struct PairCodec<float> {
   }
 };
 template <> struct PairCodec<F16Dev> {
-  __device__ static float raw(__half e) { return __half2float(e); }
+  // raw: the binary16 bits, unconverted; dec: one mixed-precision FMA per value
+  // (fma.rn.f32.f16, sm_100 family: binary16 operands, FP32 addend and result),
+  // h * 2^-12 + b rounded once -- the FP32 value of h times 2^-12 is exact, so
+  // this equals converting h and one FP32 FMA
+  __device__ static float raw(__half e) { return __uint_as_float((unsigned)__half_as_ushort(e)); }
   __device__ static float2 dec(float2 r, float2 b) {
-    return __ffma2_rn(r, make_float2(1.0f / F16_SCALE, 1.0f / F16_SCALE), b);
+    const unsigned short h0 = (unsigned short)__float_as_uint(r.x);
+    const unsigned short h1 = (unsigned short)__float_as_uint(r.y);
+    const unsigned short s = 0x0C00;  // 2^-12 = 1 / F16_SCALE in binary16
+    float d0, d1;
+    asm("fma.rn.f32.f16 %0, %1, %2, %3;" : "=f"(d0) : "h"(h0), "h"(s), "f"(b.x));
+    asm("fma.rn.f32.f16 %0, %1, %2, %3;" : "=f"(d1) : "h"(h1), "h"(s), "f"(b.y));
+    return make_float2(d0, d1);
   }
   template <int Q>
   __device__ static void put2(__half *p0, __half *p1, float2 v, float b, bool s0, bool s1,
