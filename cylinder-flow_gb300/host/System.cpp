@@ -71,6 +71,9 @@ void System::read(const std::string &path) {
     else if (key == "compute")
       pick(key, v, {{"fp64", CFLBM_COMPUTE_FP64}, {"fp32", CFLBM_COMPUTE_FP32},
                     {"df64", CFLBM_COMPUTE_DF64}}, compute);
+    else if (key == "rounding")
+      pick(key, v, {{"stochastic", CFLBM_ROUND_STOCHASTIC}, {"nearest", CFLBM_ROUND_NEAREST}},
+           rounding);
     else if (key == "geom")
       pick(key, v, {{"none", CFLBM_GEOM_NONE}, {"cylinder", CFLBM_GEOM_CYLINDER},
                     {"sphere", CFLBM_GEOM_SPHERE}}, geom);

@@ -11,8 +11,9 @@
 // solver options: lattice (9|27), profile (ref2d|ref3d|channel), storage
 // (fp64|fp32|fp16dev), compute (fp64|fp32|df64), steps (overrides the derived Time),
 // inter, geom (none|cylinder|sphere), center (cx cy cz), diam, wall_y, wall_z
-// (freeslip|noslip|periodic), perturb (amplitude), seed.  An unknown key or
-// value sets ok = false and names it in `error`.
+// (freeslip|noslip|periodic), perturb (amplitude), seed, rounding
+// (stochastic|nearest: FP16 stores).  An unknown key or value sets ok = false
+// and names it in `error`.
 #ifndef CFLBM_HOST_SYSTEM_HPP
 #define CFLBM_HOST_SYSTEM_HPP
 #include <cstdint>
@@ -36,6 +37,7 @@ class System {
   int profile = 2;  // CFLBM_PROFILE_REF3D
   int storage = 0;
   int compute = 0;
+  int rounding = 1;  // CFLBM_ROUND_STOCHASTIC
   int geom = 0;
   double cx = 0, cy = 0, cz = 0, diam = 0;
   int wall_y = 0, wall_z = 2;

@@ -22,6 +22,7 @@ void apply_input_extensions(cflbm_config &c) {
     if (k == "profile") c.profile = s.profile;
     else if (k == "storage") c.storage = s.storage;
     else if (k == "compute") c.compute = s.compute;
+    else if (k == "rounding") c.rounding = s.rounding;
     else if (k == "geom") c.geom = s.geom;
     else if (k == "center") { c.cx = s.cx; c.cy = s.cy; c.cz = s.cz; }
     else if (k == "diam") c.diam = s.diam;

@@ -20,9 +20,9 @@ int main(int argc, char **argv) {
   System s(argv[1]);
   std::printf("%d %d %d %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g %d\n", s.ok ? 1 : 0, s.sx,
               s.sy, s.sz, s.Time, s.inter, s.miu, s.u0, s.R, s.rho0, s.Ma, s.tau, s.Re);
-  std::printf("%d %d %d %d %d %.17g %.17g %.17g %.17g %d %d %.17g %llu\n", s.lattice,
+  std::printf("%d %d %d %d %d %.17g %.17g %.17g %.17g %d %d %.17g %llu %d\n", s.lattice,
               s.profile, s.storage, s.compute, s.geom, s.cx, s.cy, s.cz, s.diam, s.wall_y,
-              s.wall_z, s.perturb, (unsigned long long)s.seed);
+              s.wall_z, s.perturb, (unsigned long long)s.seed, s.rounding);
   std::printf("%s\n", s.error.c_str());
   return 0;
 }
@@ -72,13 +72,15 @@ def test_extension_keys_set_solver_options(system_exe, tmp_path):
                  "cflbm.lattice 9\ncflbm.profile channel\ncflbm.storage fp32\n"
                  "cflbm.compute fp32\ncflbm.steps 2000\ncflbm.inter 500\ncflbm.geom cylinder\n"
                  "cflbm.center 80 50 0\ncflbm.diam 20\ncflbm.wall_y noslip\n"
-                 "cflbm.wall_z periodic\ncflbm.perturb 0.001\ncflbm.seed 99\n")
+                 "cflbm.wall_z periodic\ncflbm.perturb 0.001\ncflbm.seed 99\n"
+                 "cflbm.rounding nearest\n")
     a, b = read(system_exe, p)
     assert (int(a[4]), int(a[5])) == (2000, 500)
     assert b[:5] == ["9", "0", "1", "1", "1"]
     assert [float(v) for v in b[5:9]] == [80.0, 50.0, 0.0, 20.0]
     assert b[9:11] == ["1", "2"]
     assert float(b[11]) == 0.001 and b[12] == "99"
+    assert b[13] == "0"  # CFLBM_ROUND_NEAREST (stochastic when the key is absent)
 
 
 def test_missing_input_is_reported(system_exe, tmp_path):
@@ -96,7 +98,8 @@ def test_extension_key_selects_double_float_collision(system_exe, tmp_path):
 
 @pytest.mark.parametrize("key,value", [("profile", "Channel"), ("storage", "fp16"),
                                        ("compute", "DF64"), ("geom", "disk"),
-                                       ("wall_y", "slip"), ("wall_z", "wall")])
+                                       ("wall_y", "slip"), ("wall_z", "wall"),
+                                       ("rounding", "stochastic-ish")])
 def test_unknown_extension_values_are_rejected(system_exe, tmp_path, key, value):
     p = tmp_path / "input.in"
     p.write_text("1.0  8.0  100\n0.05  100  10\n64  32  32\n=============\nrho R Re\n"
