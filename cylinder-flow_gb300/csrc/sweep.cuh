@@ -196,19 +196,45 @@ template <> __device__ __forceinline__ df64 rconst<df64>(const SweepArgs &a, int
 }
 
 
-// BGK relaxation toward the incompressible equilibrium
-//   feq_i = w_i (3p + 3 e_i.u + 4.5 (e_i.u)^2 - 1.5 |u|^2)
-// ("3D MPI+KOKKOS+MPIIO/lbm.cpp:257-272"), f <- (1 - omega) f + omega feq, with
-// omega and the weight folded into per-class constants (rconst) and written per
-// +/- pair: the pair shares e.u, (e.u)^2 and the even part of feq; the odd part
-// flips sign.  Per cell and pair k of class c:
-//   c0 = rho3 - 1.5 |u|^2,  A_c = Kw_c c0,
-//   sym = Ka_c (e.u)^2 + A_c,  asym = K3_c e.u,
-//   f_i = (1 - omega) f_i + (sym + asym),  f_opp(i) = (1 - omega) f_opp(i) + (sym - asym).
-// The corner directions' e.u reuse the face diagonals' (e_x u_x + e_y u_y).
-// D3Q27 in FP64: 110 operations per cell (151 unfolded).
-template <class L, class V, class SF>
-__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, const SweepArgs &a) {
+template <class L, int k, class V>
+__device__ __forceinline__ V pair_eu(V ux, V uy, V uz) {
+  using O = VA<V>;
+  using S = typename O::S;
+  constexpr int i = L::pair(k);
+  constexpr int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+  if constexpr (ex != 0 && ey != 0 && ez != 0) {
+    constexpr int kb = pair_of<L>(dir_of<L>(ex, ey, 0));
+    static_assert(kb >= 0 && kb < k, "face diagonal precedes the corner");
+    const V e = pair_eu<L, kb>(ux, uy, uz);
+    const V b = L::ex(L::pair(kb)) == ex ? e : O::sub(O::splat(S(0)), e);
+    return ez > 0 ? O::add(b, uz) : O::sub(b, uz);
+  } else {
+    constexpr int n = (ex != 0) + (ey != 0) + (ez != 0);
+    if constexpr (n == 1) {
+      return ex > 0 ? ux : ex < 0 ? O::sub(O::splat(S(0)), ux)
+           : ey > 0 ? uy : ey < 0 ? O::sub(O::splat(S(0)), uy)
+           : ez > 0 ? uz : O::sub(O::splat(S(0)), uz);
+    } else {
+      // two components (p, q): the positive one first
+      constexpr bool hx = ex != 0, hy = ey != 0;
+      constexpr int s1 = hx ? ex : ey, s2 = hx ? (hy ? ey : ez) : ez;
+      const V p1 = hx ? ux : uy;
+      const V p2 = hx ? (hy ? uy : uz) : uz;
+      if constexpr (s1 > 0) return s2 > 0 ? O::add(p1, p2) : O::sub(p1, p2);
+      else if constexpr (s2 > 0) return O::sub(p2, p1);
+      else return O::sub(O::sub(O::splat(S(0)), p1), p2);
+    }
+  }
+}
+
+// The BGK relaxation over a getter and a putter: get(I) returns population I
+// (a std::integral_constant index), put(I, v) receives its relaxed value, pair
+// by pair, so a caller may hold every population in registers (bgk_relax_v) or
+// fetch and store them one pair at a time.  Same operations in the same order
+// either way.
+template <class L, class V, class SF, class G, class Pt>
+__device__ __forceinline__ void bgk_relax_each(G &&get, Pt &&put, V rho3, V ux, V uy, V uz,
+                                               const SweepArgs &a) {
   using O = VA<V>;
   using S = typename O::S;
   const V omc = rconst<V>(a, RK_OMC);
@@ -223,50 +249,44 @@ __device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, cons
 #pragma unroll
   for (int c = 0; c < NC; ++c) Ac[c] = O::mul(rconst<V>(a, RK_W + c), c0);
   if constexpr (kPairs) Ac[0] = O::fma(rconst<V>(a, RK_W), c0, O::mul(rconst<V>(a, RK_LW), c0));
-  f[0] = O::fma(omc, f[0], Ac[0]);
-  V eu[L::NPAIR];
+  put(std::integral_constant<int, 0>{}, O::fma(omc, get(std::integral_constant<int, 0>{}), Ac[0]));
   static_for(
       [&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int i = L::pair(k), j = L::opp(L::pair(k));
-        constexpr int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
         constexpr int c = wclass<L>(i);
-        if constexpr (ex != 0 && ey != 0 && ez != 0) {
-          // corner: (e_x u_x + e_y u_y) of the face diagonal (e_x, e_y, 0), +- u_z
-          constexpr int kb = pair_of<L>(dir_of<L>(ex, ey, 0));
-          static_assert(kb >= 0 && kb < k, "face diagonal precedes the corner");
-          const V b = L::ex(L::pair(kb)) == ex ? eu[kb] : O::sub(O::splat(S(0)), eu[kb]);
-          eu[k] = ez > 0 ? O::add(b, uz) : O::sub(b, uz);
-        } else {
-          // sum of the nonzero signed components, led by a positive one
-          constexpr int n = (ex != 0) + (ey != 0) + (ez != 0);
-          const V cx = ux, cy = uy, cz = uz;
-          if constexpr (n == 1) {
-            eu[k] = ex > 0 ? cx : ex < 0 ? O::sub(O::splat(S(0)), cx)
-                  : ey > 0 ? cy : ey < 0 ? O::sub(O::splat(S(0)), cy)
-                  : ez > 0 ? cz : O::sub(O::splat(S(0)), cz);
-          } else {
-            // two components (p, q): the positive one first
-            constexpr bool hx = ex != 0, hy = ey != 0;
-            constexpr int s1 = hx ? ex : ey, s2 = hx ? (hy ? ey : ez) : ez;
-            const V p1 = hx ? cx : cy;
-            const V p2 = hx ? (hy ? cy : cz) : cz;
-            if constexpr (s1 > 0) eu[k] = s2 > 0 ? O::add(p1, p2) : O::sub(p1, p2);
-            else if constexpr (s2 > 0) eu[k] = O::sub(p2, p1);
-            else eu[k] = O::sub(O::sub(O::splat(S(0)), p1), p2);
-          }
-        }
-        const V e2 = O::mul(eu[k], eu[k]);
+        const V eu = pair_eu<L, k>(ux, uy, uz);
+        const V e2 = O::mul(eu, eu);
         V sym = O::fma(e2, rconst<V>(a, RK_A + c), Ac[c]);
-        V asym = O::mul(rconst<V>(a, RK_3 + c), eu[k]);
+        V asym = O::mul(rconst<V>(a, RK_3 + c), eu);
         if constexpr (kPairs && c == 1) {
           sym = O::fma(e2, rconst<V>(a, RK_LA), sym);
-          asym = O::fma(rconst<V>(a, RK_L3), eu[k], asym);
+          asym = O::fma(rconst<V>(a, RK_L3), eu, asym);
         }
-        f[i] = O::fma(omc, f[i], O::add(sym, asym));
-        f[j] = O::fma(omc, f[j], O::sub(sym, asym));
+        put(std::integral_constant<int, i>{},
+            O::fma(omc, get(std::integral_constant<int, i>{}), O::add(sym, asym)));
+        put(std::integral_constant<int, j>{},
+            O::fma(omc, get(std::integral_constant<int, j>{}), O::sub(sym, asym)));
       },
       std::make_integer_sequence<int, L::NPAIR>{});
+}
+
+// BGK relaxation toward the incompressible equilibrium
+//   feq_i = w_i (3p + 3 e_i.u + 4.5 (e_i.u)^2 - 1.5 |u|^2)
+// ("3D MPI+KOKKOS+MPIIO/lbm.cpp:257-272"), f <- (1 - omega) f + omega feq, with
+// omega and the weight folded into per-class constants (rconst) and written per
+// +/- pair: the pair shares e.u, (e.u)^2 and the even part of feq; the odd part
+// flips sign.  Per cell and pair k of class c:
+//   c0 = rho3 - 1.5 |u|^2,  A_c = Kw_c c0,
+//   sym = Ka_c (e.u)^2 + A_c,  asym = K3_c e.u,
+//   f_i = (1 - omega) f_i + (sym + asym),  f_opp(i) = (1 - omega) f_opp(i) + (sym - asym).
+// The corner directions' e.u reuse the face diagonals' (e_x u_x + e_y u_y).
+// D3Q27 in FP64: 110 operations per cell (151 unfolded).
+template <class L, class V, class SF>
+__device__ __forceinline__ void bgk_relax_v(V *f, V rho3, V ux, V uy, V uz, const SweepArgs &a) {
+  bgk_relax_each<L, V, SF>([&](auto ic) { return f[decltype(ic)::value]; },
+                           [&](auto ic, V v) { f[decltype(ic)::value] = v; }, rho3, ux, uy, uz,
+                           a);
 }
 
 template <class L, class A, class SF>
@@ -278,22 +298,22 @@ __device__ __forceinline__ void bgk_relax(A *f, A rho3, A ux, A uy, A uz, const 
 // cascade over the 3 x 3 x 3 cube of velocities -- per (e_x, e_y) line the sum
 // and the difference along z, then along y, then along x -- 49 additions for
 // D3Q27 (14 for D2Q9) instead of 66 (18) with pair sums.
-template <class L, class V, class SF>
-__device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
+template <class L, class V, class G>
+__device__ __forceinline__ void moments_get(G &&get, V &rho3, V &ux, V &uy, V &uz) {
   using O = VA<V>;
   using S = typename O::S;
   if constexpr (L::D == 3) {
     V s0[3][3], s1[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const V lo = f[dir_of<L>(a - 1, b - 1, -1)];
-        const V mid = f[dir_of<L>(a - 1, b - 1, 0)];
-        const V hi = f[dir_of<L>(a - 1, b - 1, 1)];
-        s0[a][b] = O::add(O::add(lo, hi), mid);
-        s1[a][b] = O::sub(hi, lo);
-      }
+    static_for(
+        [&](auto kc) {
+          constexpr int k = decltype(kc)::value, a = k / 3, b = k % 3;
+          const V lo = get(std::integral_constant<int, dir_of<L>(a - 1, b - 1, -1)>{});
+          const V mid = get(std::integral_constant<int, dir_of<L>(a - 1, b - 1, 0)>{});
+          const V hi = get(std::integral_constant<int, dir_of<L>(a - 1, b - 1, 1)>{});
+          s0[a][b] = O::add(O::add(lo, hi), mid);
+          s1[a][b] = O::sub(hi, lo);
+        },
+        std::make_integer_sequence<int, 9>{});
     V t00[3], t01[3], t10[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -307,19 +327,25 @@ __device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz
     uz = O::add(O::add(t10[0], t10[2]), t10[1]);
   } else {
     V s0[3], s1[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const V lo = f[dir_of<L>(a - 1, -1, 0)];
-      const V mid = f[dir_of<L>(a - 1, 0, 0)];
-      const V hi = f[dir_of<L>(a - 1, 1, 0)];
-      s0[a] = O::add(O::add(lo, hi), mid);
-      s1[a] = O::sub(hi, lo);
-    }
+    static_for(
+        [&](auto ac) {
+          constexpr int a = decltype(ac)::value;
+          const V lo = get(std::integral_constant<int, dir_of<L>(a - 1, -1, 0)>{});
+          const V mid = get(std::integral_constant<int, dir_of<L>(a - 1, 0, 0)>{});
+          const V hi = get(std::integral_constant<int, dir_of<L>(a - 1, 1, 0)>{});
+          s0[a] = O::add(O::add(lo, hi), mid);
+          s1[a] = O::sub(hi, lo);
+        },
+        std::make_integer_sequence<int, 3>{});
     rho3 = O::add(O::add(s0[0], s0[2]), s0[1]);
     ux = O::sub(s0[2], s0[0]);
     uy = O::add(O::add(s1[0], s1[2]), s1[1]);
     uz = O::splat(S(0));
   }
+}
+template <class L, class V, class SF>
+__device__ __forceinline__ void moments(const V *f, V &rho3, V &ux, V &uy, V &uz) {
+  moments_get<L, V>([&](auto ic) { return f[decltype(ic)::value]; }, rho3, ux, uy, uz);
 }
 
 // Macros out (when requested), Brinkman damping of the equilibrium velocity,
