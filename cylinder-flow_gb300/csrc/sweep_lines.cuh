@@ -5,7 +5,7 @@
 // Why: with 2-byte populations a warp-wide load moves 64 bytes, and the
 // register-fed two-cell kernel (sweep_channel2_kernel) cannot keep enough of
 // them in flight to reach the copy bandwidth -- it is bound by latency, not by
-// DRAM.  Here one thread of a block issues, per line, one bulk copy per
+// DRAM.  Here the lanes of a producer warp issue, per line, one bulk copy per
 // population: the whole source row of that population (ROWS layout: the Q rows
 // of a line are adjacent, each row is contiguous and starts on a 128-byte
 // boundary), ~1 KB per copy for a 512-cell line, into a ring of stages; the
@@ -22,6 +22,11 @@
 // step); solid cells get p = u = 0.  The arithmetic is channel2_cells' (packed
 // FP32x2, two cells per thread: x and x + 32 of a 64-cell warp span), so the
 // states are bit-identical to the register-fed kernel's.
+//
+// Measured on GB300 it is the slower of the two (0.31 against 0.59 of the copy
+// peak at 512x128x128): it removes most of the load latency but executes about
+// a third more instructions per cell, so it runs only on request
+// (CFLBM_FP16_SWEEP=lines).
 //
 // A producer warp issues the copies (and the line's listed-tile positions and
 // link words) into a ring of stages; eight consumer warps compute.  Stages are
