@@ -311,6 +311,25 @@ def test_layouts_give_identical_states(cuda, name, storage):
     assert np.array_equal(out[0][1], out[1][1])
 
 
+@pytest.mark.parametrize("name", ["d3q27_cyl", "d3q27_noslip"])
+@pytest.mark.parametrize("rounding", ["stochastic", "nearest"])
+def test_line_staged_sweep_matches_pair_kernel(cuda, name, rounding, monkeypatch):
+    """The opt-in line-staged FP16 sweep (CFLBM_FP16_SWEEP=lines, read when a
+    handle is created) gives the register-fed pair kernel's states and forces
+    bit for bit, no-slip faces and solid links included."""
+    case = CHANNEL_CASES[name]
+    out = []
+    for mode in ("registers", "lines"):
+        monkeypatch.setenv("CFLBM_FP16_SWEEP", mode)
+        with Solver(perturb_amp=1e-3, layout="rows", storage="fp16dev", compute="fp32",
+                    rounding=rounding, **case) as s:
+            s.step(12)
+            s.synchronize()
+            out.append((s.get_f(), s.force_history()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 def test_reference_profile_rows_layout_matches_golden(cuda):
     g = load_golden("ref3d_40x12x12")
     m = g["meta"]
