@@ -88,11 +88,13 @@ def test_config_default():
     assert cfg.lattice == 9 and cfg.nx == 64 and cfg.ny == 32
     assert cfg.storage == C.STORE_FP64 and cfg.compute == C.COMPUTE_FP64
     assert cfg.tau0 == 0.03 and cfg.u0 == 0.05
+    assert cfg.layout == C.LAYOUT_ROWS and cfg.rounding == C.ROUND_STOCHASTIC
 
 
 @pytest.mark.parametrize("field,value", [("lattice", 7), ("nx", 2), ("storage", 9),
                                          ("compute", 5), ("profile", 4), ("wall_y", 3),
-                                         ("tau0", -0.6), ("force_history", -1)])
+                                         ("tau0", -0.6), ("force_history", -1),
+                                         ("layout", 2), ("rounding", 2)])
 def test_create_rejects_bad_config_before_touching_the_gpu(field, value):
     cfg = C.Config()
     C.lib.cflbm_config_default(ctypes.byref(cfg))
