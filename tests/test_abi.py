@@ -148,6 +148,30 @@ def test_strouhal_of_a_pure_tone():
     assert abs(st - 20.0 / period / 0.05) < 2e-3
 
 
+def test_drag_over_whole_shedding_periods():
+    """A window that ends mid-cycle moves the plain mean of a drag oscillating
+    at twice the shedding frequency; the mean over whole periods (the period
+    from the periodogram peak, within a fraction of a percent over 4.7 cycles)
+    moves far less."""
+    diam, u0, period = 20.0, 0.05, 2040.0
+    n = int(4.7 * period)
+    t = np.arange(n)
+    q = 0.5 * u0 * u0 * diam
+    cl = 0.5 * np.sin(2 * np.pi * t / period)
+    cd = 1.82 + 0.05 * np.sin(4 * np.pi * t / period)
+    force = np.stack([cd * q, cl * q, np.zeros(n)], axis=1)
+    a, k = cflbm.analysis.shedding_window(cl, diam, u0)
+    assert k == 4 and abs((n - a) - 4 * period) <= 0.005 * 4 * period
+    st = cflbm.analysis.summary(force, u0, diam, diam, n)
+    assert st["periods"] == 4
+    assert abs(st["cd_mean"] - 1.82) > 1e-3  # the plain mean: 1.5e-3 off
+    assert abs(st["cd_mean_periods"] - 1.82) < 2e-4
+    # no oscillation: the whole-period mean falls back to the plain mean
+    flat = np.stack([np.full(n, 1.5 * q), np.zeros(n), np.zeros(n)], axis=1)
+    st0 = cflbm.analysis.summary(flat, u0, diam, diam, n)
+    assert st0["periods"] == 0 and st0["cd_mean_periods"] == st0["cd_mean"]
+
+
 def test_test_dat_format(tmp_path):
     p = str(tmp_path / "test.dat")
     cflbm.analysis.write_test_dat(p, np.array([[1.25, -0.5]]), append=False)
