@@ -466,8 +466,10 @@ template <> struct PairT<float2> {
   __device__ static float third(float c) { return __fmul_rn(c, 1.0f / 3.0f); }
 };
 
-// Storage codec of a cell pair on FP32x2 (the two-cell kernels): the raw
-// elements convert one by one and the FP16 format's offset and scale apply to
+// Storage codec of a cell pair on FP32x2 (the two-cell kernels): raw() takes
+// an element as loaded (FP64 converted to FP32; FP16 kept as its bits) and
+// dec() forms the pair's FP32 values -- for FP16 one mixed-precision FMA per
+// value, h 2^-12 + b; the encode applies the FP16 format's offset and scale to
 // the pair in one packed FMA -- the same values as Store<>::load/store per cell
 // (the product with a power of two is exact, so fma(v, 2^12, -2^12 b) is
 // 2^12 (v - b) rounded once).  `key` is the first value's element (cell * Q +
