@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(32 * BY, SOLID ? 16 / BY + 1 : 24 / BY)
       const unsigned rf = ((unsigned)wk.y >> 16) >> (2 * wid);
       const bool act0 = rf & 1u, act1 = (rf >> 1) & 1u;
       if (act0 || act1)  // warp-uniform
-        channel2_cells<Q, ST, float2>(a, 64 * pair + lane, y, z, act0, act1);
+        channel2_cells<Q, ST, float2, false, false>(a, 64 * pair + lane, y, z, act0, act1);
       continue;
     }
     double Fx = 0.0, Fy = 0.0, Fz = 0.0;
@@ -224,8 +224,8 @@ __global__ void __launch_bounds__(32 * BY, MINB)
   const unsigned rf = ((unsigned)wk.y >> 16) >> (2 * wid);
   const bool act0 = rf & 1u, act1 = (rf >> 1) & 1u;
   if (act0 || act1)  // warp-uniform
-    channel2_cells<Q, ST, float2>(a, 64 * (wk.y & 0xffff) + threadIdx.x, wk.z * BY + wid, wk.w, act0,
-                          act1);
+    channel2_cells<Q, ST, float2, false, false>(a, 64 * (wk.y & 0xffff) + threadIdx.x,
+                                                wk.z * BY + wid, wk.w, act0, act1);
 }
 
 // grid > 0: persistent grids of `grid` blocks for both kinds of work; grid = 0:

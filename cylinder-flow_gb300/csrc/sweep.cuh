@@ -649,7 +649,10 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
 // at 2-3 blocks per SM it ran at 2.9-3.9 G cell updates/s against 7.5 for one
 // cell per thread at 5 blocks per SM, D3Q27 512x128x128.)  A pair holding a listed
 // tile pulls through pull_pair_listed (face-state tables and link words).
-template <int Q, class ST, class P, int I>
+// POFF: the source offset from the kernel-parameter table a.poff (when `a` is a
+// kernel parameter); otherwise formed from the layout strides (when `a` sits in
+// global or shared memory, as in the batch, where the table would be a load).
+template <int Q, class ST, class P, int I, bool POFF = true>
 __device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restrict__ p,
                                        const typename Store<ST>::elem *__restrict__ pm0,
                                        const typename Store<ST>::elem *__restrict__ pm1,
@@ -657,7 +660,9 @@ __device__ __forceinline__ P pull_pair(const typename Store<ST>::elem *__restric
                                        bool act1, bool inlet0, const SweepArgs &a) {
   using Dd = DirC<Q, I>;
   using PC = PairCodec<ST>;
-  const long long off = a.poff[I];
+  long long off;
+  if constexpr (POFF) off = a.poff[I];
+  else off = I * S - (Dd::ex + Dd::ey * rs + Dd::ez * zs);
   float r0 = 0.0f, r1 = 0.0f;
   if constexpr (Dd::ex < 0) {  // the outlet column repeats itself (pm = p - 1 there)
     if (act0) r0 = PC::raw(__ldg(pm0 + off));
@@ -709,7 +714,7 @@ __device__ __forceinline__ P pull_pair_listed(const typename Store<ST>::elem *__
 // LISTED: the pair holds a listed tile; both cells pull through the face-state
 // tables and their link words l0 / l1 (bit 31: solid cell), act0 = true and
 // act1 = the second tile exists.
-template <int Q, class ST, class P, bool LISTED = false>
+template <int Q, class ST, class P, bool LISTED = false, bool POFF = true>
 __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y, int z,
                                                bool act0, bool act1, unsigned l0 = 0u,
                                                unsigned l1 = 0u) {
@@ -745,7 +750,8 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
     static_for(
         [&](auto ic) {
           constexpr int I = decltype(ic)::value;
-          f[I] = pull_pair<Q, ST, P, I>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1, inlet0, a);
+          f[I] = pull_pair<Q, ST, P, I, POFF>(p, pm0, pm1, S, a.L.rs, a.L.zs, act0, act1,
+                                              inlet0, a);
         },
         std::make_integer_sequence<int, Q>{});
   }
