@@ -86,6 +86,7 @@ SIGNATURES = {
     "cflbm_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "cflbm_step": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "cflbm_synchronize": ([ctypes.c_void_p], ctypes.c_int),
+    "cflbm_selftest_wait_timeout": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "cflbm_macros": ([ctypes.c_void_p, _dp, _dp, _dp, _dp], ctypes.c_int),
     "cflbm_macros_device": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),

@@ -844,6 +844,15 @@ int cflbm_synchronize(cflbm_handle *h) {
   return check_device_error(h);
 }
 
+int cflbm_selftest_wait_timeout(cflbm_handle *h, int64_t polls) {
+  if (!h) return fail(CFLBM_E_INVALID, "handle is NULL");
+  if (polls < 1 || polls > (int64_t)1 << 22)
+    return fail(CFLBM_E_INVALID, "polls = %lld outside [1, 2^22]", (long long)polls);
+  CK_CUDA(cudaSetDevice(h->cfg.device));
+  CK_CUDA(launch_wait_timeout_probe(h->d_err, (long long)polls, h->stream));
+  return CFLBM_OK;
+}
+
 // Channel profile: forms u, v, w, p of the last step from the state that step
 // read (fB after the step; intact until the next step), once per step.
 static int ensure_macros(cflbm_handle *h) {

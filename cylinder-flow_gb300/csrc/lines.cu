@@ -58,4 +58,22 @@ cudaError_t launch_lines_f16_q27(const SweepArgs &a, int sms, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Self-test of the bounded-wait error path: one thread waits on an mbarrier
+// that nothing arrives on, gives up after `polls` polls and records
+// LINES_TIMEOUT in *err, as a sweep's wait would.  No copy is in flight, so
+// the kernel simply returns.
+__global__ void wait_timeout_probe_kernel(unsigned *err, long long polls) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!mbar_wait_bounded(&bar, 0u, polls)) atomicExch(err, LINES_TIMEOUT);
+  }
+}
+
+cudaError_t launch_wait_timeout_probe(unsigned *err, long long polls, cudaStream_t s) {
+  wait_timeout_probe_kernel<<<1, 32, 0, s>>>(err, polls);
+  return cudaGetLastError();
+}
+
 }  // namespace cflbm

@@ -200,6 +200,7 @@ void set_offsets(SweepArgs &a, int Q);
 bool lines_supported(int Q, int store, int layout_rows, bool alpha, int nx);
 cudaError_t lines_prepare();
 cudaError_t launch_lines_f16_q27(const SweepArgs &a, int sms, cudaStream_t s);
+cudaError_t launch_wait_timeout_probe(unsigned *err, long long polls, cudaStream_t s);
 
 // Number of kernel launches issued through the launchers (all handles).
 long long launches();

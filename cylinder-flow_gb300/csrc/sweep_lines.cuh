@@ -74,8 +74,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
-  for (long long k = 0; k < LINES_SPIN_LIMIT; ++k)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
+                                                  long long limit = LINES_SPIN_LIMIT) {
+  for (long long k = 0; k < limit; ++k)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

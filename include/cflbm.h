@@ -141,6 +141,15 @@ int cflbm_step(cflbm_handle *h, int nsteps);
 /* Block until all work queued on the handle's stream has finished. */
 int cflbm_synchronize(cflbm_handle *h);
 
+/* Self-test of the bounded-wait error path (no reference counterpart): queues
+ * on h's stream a kernel whose one waiting thread gives up on an mbarrier that
+ * nothing arrives on after `polls` polls (1 .. 2^22) and records the timeout
+ * in h's device error word, as the line-staged sweep's waits do.  The next
+ * synchronising call (cflbm_synchronize, cflbm_mass) then returns
+ * CFLBM_E_CUDA naming the timeout, and every later one does too: the handle is
+ * marked failed; destroy it.  The CUDA context stays usable. */
+int cflbm_selftest_wait_timeout(cflbm_handle *h, int64_t polls);
+
 /* Macroscopic fields after the last step: u, v, w, p over the interior, x
  * fastest, as LBM::Update leaves them ("3D.../lbm.cpp:374-417": p = sum f/3,
  * u = sum f e, zero in solids, reference-profile inlet/outlet overrides).

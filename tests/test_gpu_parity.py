@@ -18,6 +18,7 @@ from oracle import oracle as O
 
 import cflbm
 from cflbm import Batch, Solver
+from cflbm import _lib as C
 
 pytestmark = pytest.mark.gpu
 
@@ -405,3 +406,22 @@ def test_forces_async_matches_forces(cuda):
     assert np.array_equal(out[0].numpy(), np.zeros(3))
     assert np.array_equal(out[1:].numpy(), hist[:5])
     assert np.array_equal(out[5].numpy(), f)
+
+
+def test_bounded_wait_timeout_reaches_the_host(cuda):
+    """The bounded-wait error path of the line-staged sweep, made to run out on
+    purpose with an mbarrier that nothing arrives on (no copy in flight): the
+    next synchronising call reports the timeout, the handle stays failed, and
+    the CUDA context stays usable for a new handle."""
+    case = CHANNEL_CASES["d3q27_cyl"]
+    with Solver(storage="fp16dev", compute="fp32", **case) as s:
+        s.step(2)
+        s.synchronize()
+        assert C.lib.cflbm_selftest_wait_timeout(s._h, 1000) == 0
+        assert C.lib.cflbm_synchronize(s._h) != 0
+        assert b"timed out" in C.lib.cflbm_last_error()
+        assert C.lib.cflbm_synchronize(s._h) != 0
+    with Solver(storage="fp16dev", compute="fp32", **case) as s:
+        s.step(2)
+        s.synchronize()
+        assert np.all(np.isfinite(s.get_f()))
