@@ -210,6 +210,42 @@ __global__ void tile_list_kernel(const SetupArgs s, const unsigned char *flag,
   }
 }
 
+// One warp per listed tile t: flag[t] = 1 when a fluid cell of the tile has
+// solid links.
+__global__ void force_flags_kernel(int n_slow, const uint32_t *links_bits, unsigned char *flag) {
+  const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= n_slow) return;  // warp-uniform
+  const unsigned word = links_bits[t * 32 + lane];
+  const bool f = __any_sync(0xffffffffu, (word & 0x7fffffffu) != 0u && !(word >> 31));
+  if (lane == 0) flag[t] = f ? 1 : 0;
+}
+
+// Per chunk of TILES_PER_CHUNK flags: their count.
+__global__ void flag_count_kernel(int n, const unsigned char *flag, int *chunk) {
+  __shared__ int sh[SETUP_THREADS / 32];
+  const long long t0 = (long long)blockIdx.x * TILES_PER_CHUNK + threadIdx.x * TILES_PER_THREAD;
+  int c = 0;
+  for (int k = 0; k < TILES_PER_THREAD; ++k)
+    if (t0 + k < n) c += flag[t0 + k];
+  int total;
+  (void)block_exclusive_sum(c, sh, total);
+  if (threadIdx.x == 0) chunk[blockIdx.x] = total;
+}
+
+// Per chunk: the flagged positions at the chunk's offset, in order.
+__global__ void flag_list_kernel(int n, const unsigned char *flag, const int *chunk, int *out) {
+  __shared__ int sh[SETUP_THREADS / 32];
+  const long long t0 = (long long)blockIdx.x * TILES_PER_CHUNK + threadIdx.x * TILES_PER_THREAD;
+  int c = 0;
+  for (int k = 0; k < TILES_PER_THREAD; ++k)
+    if (t0 + k < n) c += flag[t0 + k];
+  int total;
+  int pos = chunk[blockIdx.x] + block_exclusive_sum(c, sh, total);
+  for (int k = 0; k < TILES_PER_THREAD; ++k)
+    if (t0 + k < n && flag[t0 + k]) out[pos++] = (int)(t0 + k);
+}
+
 int grid_for(long long n) {
   long long b = (n + SETUP_THREADS - 1) / SETUP_THREADS;
   return (int)std::max<long long>(1, std::min<long long>(b, 65535LL * 16));
@@ -248,6 +284,25 @@ cudaError_t launch_setup_list(const SetupArgs &s, const unsigned char *flag, con
   tile_list_kernel<<<setup_chunks(s), SETUP_THREADS, 0, st>>>(s, flag, chunk, mask, bits,
                                                                tile_index, list, links_bits);
   count_launch();
+  return cudaGetLastError();
+}
+
+int force_chunks(int n_slow) {
+  return std::max(1, (n_slow + TILES_PER_CHUNK - 1) / TILES_PER_CHUNK);
+}
+
+cudaError_t launch_setup_force_list(const SetupArgs &s, int n_slow, const uint32_t *links_bits,
+                                    unsigned char *flag, int *chunk, int *total,
+                                    int *force_list, cudaStream_t st) {
+  (void)s;
+  const int nchunks = force_chunks(n_slow);
+  if (n_slow > 0)
+    force_flags_kernel<<<(unsigned)((32LL * n_slow + SETUP_THREADS - 1) / SETUP_THREADS),
+                         SETUP_THREADS, 0, st>>>(n_slow, links_bits, flag);
+  flag_count_kernel<<<nchunks, SETUP_THREADS, 0, st>>>(n_slow, flag, chunk);
+  chunk_scan_kernel<<<1, SETUP_THREADS, 0, st>>>(chunk, nchunks, total);
+  flag_list_kernel<<<nchunks, SETUP_THREADS, 0, st>>>(n_slow, flag, chunk, force_list);
+  count_launch(n_slow > 0 ? 4 : 3);
   return cudaGetLastError();
 }
 

@@ -27,4 +27,12 @@ cudaError_t launch_setup_list(const SetupArgs &s, const unsigned char *flag, con
                               const uint32_t *mask, const uint32_t *bits, int *tile_index,
                               int *list, uint32_t *links_bits, cudaStream_t st);
 
+// The positions in the list of the listed tiles with force work (a fluid cell
+// with solid links), in list (= tile) order; its length into *total.  flag:
+// n_slow bytes; chunk: force_chunks(n_slow) ints.
+int force_chunks(int n_slow);
+cudaError_t launch_setup_force_list(const SetupArgs &s, int n_slow, const uint32_t *links_bits,
+                                    unsigned char *flag, int *chunk, int *total,
+                                    int *force_list, cudaStream_t st);
+
 }  // namespace cflbm

@@ -88,6 +88,8 @@ struct SweepArgs {
   const int *slow_tiles; // list of tiles next to solids (tile = (z*ny + y)*nxw + x/32)
   const int *tile_index; // per warp tile: its position in slow_tiles, -1 if not listed
   int n_slow;            // length of the list
+  const int *force_tiles;  // list positions of the tiles with force work (tile order)
+  int n_force;             // its length
   const unsigned *links_bits;  // per listed tile, 32 cells: bit i = source of i is solid,
                                // bit 31 = the cell is solid
   const long long *face_off;   // [16][Q] listed-tile pull offsets per face state

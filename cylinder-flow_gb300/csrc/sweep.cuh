@@ -810,13 +810,16 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
   const int t0 = a.tile_index[trow + w0];
   const int t1 = has1 ? a.tile_index[trow + w0 + 1] : -1;
   const int x0 = 32 * w0 + threadIdx.x;
-  if (t0 < 0 && t1 < 0) {  // warp-uniform
-    channel2_cells<Q, ST, P>(a, x0, y, z, true, has1);
-  } else {
+  // The listed pair returns from its own inlined copy of the pair body: with
+  // the two copies in an if / else the kernel spilled 196 bytes, in this form
+  // 60 (FP16 storage, 96 registers).
+  if (t0 >= 0 || t1 >= 0) {  // warp-uniform
     const unsigned l0 = t0 >= 0 ? a.links_bits[(long long)t0 * SWEEP_BX + threadIdx.x] : 0u;
     const unsigned l1 = t1 >= 0 ? a.links_bits[(long long)t1 * SWEEP_BX + threadIdx.x] : 0u;
     channel2_cells<Q, ST, P, true>(a, x0, y, z, true, has1, l0, l1);
+    return;
   }
+  channel2_cells<Q, ST, P>(a, x0, y, z, true, has1);
 }
 
 // Channel sweep, one cell per thread, one warp tile per warp, over the whole
@@ -939,7 +942,8 @@ __device__ __forceinline__ void force_to_history(const SweepArgs &a, double dx, 
 
 // Momentum-exchange force on the solids for this step: a small persistent grid
 // (about one block per SM) on a second stream beside the sweep strides over
-// the listed tiles and, for every fluid cell with solid links, reads the
+// the listed tiles with force work (fluid cells with solid links; the set-up's
+// list, in tile order) and, for every fluid cell with solid links, reads the
 // populations the sweep bounces back (f*_{opp(I)}(X) from the state it pulls
 // from); per cell the sum runs in the arithmetic type, over cells in FP64.
 template <int Q, class ST, class A, int MINB>
@@ -952,10 +956,10 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) channel_force_kerne
   const long long S = a.L.S;
   const E *__restrict__ fa = static_cast<const E *>(a.fa);
   double dx = 0.0, dy = 0.0, dz = 0.0;
-  for (long long base = (long long)blockIdx.x * SWEEP_BY; base < a.n_slow;
+  for (long long base = (long long)blockIdx.x * SWEEP_BY; base < a.n_force;
        base += (long long)gridDim.x * SWEEP_BY) {
-    const long long t = base + wid;
-    if (t >= a.n_slow) continue;  // warp-uniform
+    if (base + wid >= a.n_force) continue;  // warp-uniform
+    const long long t = a.force_tiles[base + wid];
     const unsigned word = a.links_bits[t * SWEEP_BX + lane];
     const unsigned links = word & ~(1u << 31);
     A Fx = A(0), Fy = A(0), Fz = A(0);
