@@ -639,6 +639,41 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
       std::make_integer_sequence<int, Q>{});
 }
 
+// One cell of a listed tile in the arithmetic type A: the pull through the
+// face-state tables and the link word (bit 31: a solid cell, whose p and u are
+// zero), moments, BGK and the store; x >= nx loads the last column and stores
+// nothing.
+template <int Q, class ST, class A>
+__device__ __forceinline__ void channel_listed_cell(const SweepArgs &a, int x, int y, int z,
+                                                    unsigned links) {
+  using L = Lat<Q>;
+  using SF = Store<ST>;
+  using E = typename SF::elem;
+  const int nx = a.L.nx, ny = a.L.ny;
+  const bool valid = x < nx;
+  if (!valid) x = nx - 1;
+  const long long S = a.L.S;
+  const long long c = a.L.idx(x, y, z);
+  const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  const int st = face_state(y, z, ny, a.L.nz);
+  const long long *__restrict__ offs = a.face_off + st * Q;
+  const unsigned wbb = a.face_bb[st];
+  A f[Q];
+  static_for(
+      [&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        f[I] = pull_listed<Q, ST, A, I>(fa, c, S, x, offs[I], (wbb >> I) & 1u, links, a);
+      },
+      std::make_integer_sequence<int, Q>{});
+  A rho3, ux, uy, uz;
+  moments<L, A, SF>(f, rho3, ux, uy, uz);
+  if (links >> 31) {
+    rho3 = A(0); ux = A(0); uy = A(0); uz = A(0);
+  }
+  const long long cell = ((long long)z * ny + y) * nx + x;
+  finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, static_cast<E *>(a.fb), c, S, a);
+}
+
 // Interior channel sweep with two cells per thread and packed FP32x2
 // arithmetic: a warp takes the two warp tiles 2b and 2b + 1 of a row, so a thread
 // owns cells x and x + 32, whose loads and stores share their address (the
@@ -648,7 +683,10 @@ __device__ __forceinline__ void cell_force(const A *f, unsigned links, A &fx, A 
 // double-float pair type needs ~250 registers for two cells' 27 populations;
 // at 2-3 blocks per SM it ran at 2.9-3.9 G cell updates/s against 7.5 for one
 // cell per thread at 5 blocks per SM, D3Q27 512x128x128.)  A pair holding a listed
-// tile pulls through pull_pair_listed (face-state tables and link words).
+// tile pulls through pull_pair_listed (face-state tables and link words), or,
+// with LISTED1 in the kernel, takes its two cells one after the other through
+// channel_listed_cell (the same values: lane for lane the packed operations
+// are the scalar ones).
 // POFF: the source offset from the kernel-parameter table a.poff (when `a` is a
 // kernel parameter); otherwise formed from the layout strides (when `a` sits in
 // global or shared memory, as in the batch, where the table would be a load).
@@ -798,7 +836,7 @@ __device__ __forceinline__ void channel2_cells(const SweepArgs &a, int x0, int y
                                     (unsigned)(cell0 * Q + i), a.f16_sr);
 }
 
-template <int Q, class ST, class P, int MINB>
+template <int Q, class ST, class P, int MINB, bool LISTED1 = false>
 __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
     sweep_channel2_kernel(const SweepArgs a) {
   const int ny = a.L.ny;
@@ -810,13 +848,19 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB)
   const int t0 = a.tile_index[trow + w0];
   const int t1 = has1 ? a.tile_index[trow + w0 + 1] : -1;
   const int x0 = 32 * w0 + threadIdx.x;
-  // The listed pair returns from its own inlined copy of the pair body: with
-  // the two copies in an if / else the kernel spilled 196 bytes, in this form
-  // 60 (FP16 storage, 96 registers).
+  // A listed pair returns from its own inlined code: with the packed listed
+  // and plain bodies in an if / else the FP16 kernel spilled 196 bytes, in
+  // this form 60.
   if (t0 >= 0 || t1 >= 0) {  // warp-uniform
     const unsigned l0 = t0 >= 0 ? a.links_bits[(long long)t0 * SWEEP_BX + threadIdx.x] : 0u;
     const unsigned l1 = t1 >= 0 ? a.links_bits[(long long)t1 * SWEEP_BX + threadIdx.x] : 0u;
-    channel2_cells<Q, ST, P, true>(a, x0, y, z, true, has1, l0, l1);
+    if constexpr (LISTED1) {
+#pragma unroll 1
+      for (int h = 0; h < (has1 ? 2 : 1); ++h)
+        channel_listed_cell<Q, ST, typename PairT<P>::C>(a, x0 + 32 * h, y, z, h ? l1 : l0);
+    } else {
+      channel2_cells<Q, ST, P, true>(a, x0, y, z, true, has1, l0, l1);
+    }
     return;
   }
   channel2_cells<Q, ST, P>(a, x0, y, z, true, has1);
@@ -1101,21 +1145,31 @@ void launch_interior(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s) 
     }
   }
   if constexpr (sizeof(A) == 4 && !std::is_same<ST, double>::value) {
-    // Blocks per SM, measured on the D3Q27 bench step: FP32 storage 0.850 /
-    // 0.908 / 0.937 of the copy peak at 4 / 5 / 6 per SM (80 registers, no
-    // spills at 6; 7 and 8 spill); FP16 0.613 / 0.636 / 0.632 (96 registers
-    // and a 44-byte spill at 5).  D2Q9 on grids of 2^20 cells and more: 10 per
-    // SM (48 registers, no spill; 8192x1024: FP32 storage 0.982 against 0.946
-    // at 6, FP16 0.729 against 0.659); on smaller grids, which are bound by
-    // per-thread latency, 6 (640x160 FP32: 6.1 us per step against 6.6 at 10).
-    constexpr int M2 = std::is_same<ST, float>::value ? 6 : 5;
+    // Blocks per SM, measured on the D3Q27 bench step with packed listed
+    // pairs: FP32 storage 0.850 / 0.908 / 0.937 of the copy peak at 4 / 5 / 6
+    // per SM (7 and 8 spill more); FP16 0.613 / 0.636 / 0.632.  D2Q9 on grids
+    // of 2^20 cells and more: 10 per SM (48 registers; 8192x1024: FP32 storage
+    // 0.982 against 0.946 at 6, FP16 0.729 against 0.659); smaller D2Q9 grids
+    // are bound by per-thread latency (640x160 FP32: 6.1 us per step at 6
+    // against 6.6 at 10).
     dim3 g2((a.nxw + 1) / 2, grid.y, grid.z);
-    bool wide = false;
     if constexpr (Q == 9) {
-      wide = (long long)a.L.nx * a.L.ny * a.L.nz >= (1LL << 20);
-      if (wide) sweep_channel2_kernel<Q, ST, float2, 10><<<g2, block, 0, s>>>(a);
+      if ((long long)a.L.nx * a.L.ny * a.L.nz >= (1LL << 20)) {
+        sweep_channel2_kernel<Q, ST, float2, 10><<<g2, block, 0, s>>>(a);
+        return;
+      }
     }
-    if (!wide) sweep_channel2_kernel<Q, ST, float2, M2><<<g2, block, 0, s>>>(a);
+    // Listed pairs: packed (both cells at once) or one cell after the other
+    // (LISTED1; fewer live registers).  One cell at a time, measured on the
+    // channel steps: FP16 D3Q27 39.5 against 37.5 G cell updates/s on
+    // 512x128x128 and 47.4 against 45.3 on 768x384x384 (5 per SM; 37.9 / 46.4
+    // at 6), FP32 D2Q9 400x100 6.66 against 6.46 (5 per SM); FP32 D3Q27 the
+    // same either way (31.0 / 32.2 at 6 per SM); the wide D2Q9 grids 1-2 %
+    // slower (8192x1024: FP16 129.5 against 130.8, FP32 91.4 against 93.3).
+    if constexpr (Q == 27 && std::is_same<ST, float>::value)
+      sweep_channel2_kernel<Q, ST, float2, 6><<<g2, block, 0, s>>>(a);
+    else
+      sweep_channel2_kernel<Q, ST, float2, 5, true><<<g2, block, 0, s>>>(a);
   } else {
     sweep_channel_kernel<Q, ST, A, MINB_FAST><<<grid, block, 0, s>>>(a);
   }
