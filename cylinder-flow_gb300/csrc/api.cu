@@ -64,7 +64,7 @@ void free_handle(cflbm_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->fA,    h->fB,     h->d_mask, h->d_links, h->d_mu,      h->d_mv,
                   h->d_links_bits, h->d_tile_slow, h->d_slow_tiles, h->d_tile_index,
-                  h->d_face_off, h->d_face_bb, h->d_force_tiles,
+                  h->d_face_off, h->d_face_bb, h->d_bcell_idx, h->d_bcell_links,
                   h->d_mw,  h->d_mp,   h->d_inlet, h->d_alpha, h->d_fin,    h->d_hist,
                   h->d_step, h->d_partials, h->d_counter, h->d_counter2, h->d_sums,
                   h->d_err};
@@ -446,23 +446,26 @@ int cflbm_create(const cflbm_config *cfg, cflbm_handle **out) {
     if ((rc = dev_alloc_t(h, &h->d_links_bits, 32 * (size_t)total + 32))) return rc;
     CK_CUDA(launch_setup_list(sa, h->d_tile_slow, chunk, h->d_mask, bits, h->d_tile_index,
                               h->d_slow_tiles, h->d_links_bits, h->stream));
-    // the force kernel's tiles: about 9,000 of the 17,000 listed tiles of the
-    // D3Q27 512x128x128 cylinder (the others are face rows); over the whole
-    // list the force launch took 65 us, a third of the FP16 sweep beside it
-    if ((rc = dev_alloc_t(h, &h->d_force_tiles, (size_t)total + 1))) return rc;
-    const int wch = force_chunks(total);
+    // The force launch's cells: the fluid cells with solid links, one thread
+    // each.  One warp per listed tile with such cells (about 9,000 of the
+    // 17,000 listed tiles of the D3Q27 512x128x128 cylinder) left most lanes
+    // idle and held its registers for 53 us per step beside the FP16 sweep.
+    const int wch = bcell_chunks(total);
     unsigned char *wscr = nullptr;
     const size_t w_off = ((size_t)total + 256) / 256 * 256;
     CK_CUDA(cudaMalloc(&wscr, w_off + 4 * ((size_t)wch + 1)));
     std::unique_ptr<unsigned char, cudaError_t (*)(void *)> wscr_guard(wscr, cudaFree);
     int *wchunk = reinterpret_cast<int *>(wscr + w_off);
     int *wtot = wchunk + wch;
-    CK_CUDA(launch_setup_force_list(sa, total, h->d_links_bits, wscr, wchunk, wtot,
-                                    h->d_force_tiles, h->stream));
-    int wt = 0;
-    CK_CUDA(cudaMemcpyAsync(&wt, wtot, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK_CUDA(cudaStreamSynchronize(h->stream));  // the scratch is freed at scope end
-    h->n_force = wt;
+    CK_CUDA(launch_setup_bcell_count(total, h->d_links_bits, wscr, wchunk, wtot, h->stream));
+    int nb = 0;
+    CK_CUDA(cudaMemcpyAsync(&nb, wtot, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK_CUDA(cudaStreamSynchronize(h->stream));
+    h->n_bcells = nb;
+    if ((rc = dev_alloc_t(h, &h->d_bcell_idx, (size_t)nb + 1))) return rc;
+    if ((rc = dev_alloc_t(h, &h->d_bcell_links, (size_t)nb + 1))) return rc;
+    CK_CUDA(launch_setup_bcell_list(L, h->nxw, total, h->d_slow_tiles, h->d_links_bits, wscr,
+                                    wchunk, h->d_bcell_idx, h->d_bcell_links, h->stream));
     std::vector<long long> foff;
     std::vector<uint32_t> fbb;
     if (d3) face_tables<27>(L, cfg->wall_y, cfg->wall_z, foff, fbb);
@@ -677,13 +680,11 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
     sa.f_in_f[i] = (float)h->f_in[i];
     sa.f_in_l[i] = (float)(h->f_in[i] - (double)sa.f_in_f[i]);
   }
-  // Persistent grid of the force launch beside the sweep: one block per SM
-  // (measured on the D3Q27 512x128x128 bench step: 1 / 2 / 4 per SM give FP32
-  // storage 31.07 / 30.97 / 30.74, FP16 41.72 / 41.48 / 41.12, FP64 15.80 /
-  // 15.73 / 15.67 G cell updates/s).
-  const int per_sm = 1;
+  // Grid of the force launch beside the sweep: one boundary cell per thread,
+  // at most one block per SM.
+  const long long fthreads = SWEEP_BX * SWEEP_BY;
   sa.bnd_blocks = (int)std::max<long long>(
-      1, std::min<long long>((h->n_force + SWEEP_BY - 1) / SWEEP_BY, (long long)per_sm * h->sms));
+      1, std::min<long long>((h->n_bcells + fthreads - 1) / fthreads, (long long)h->sms));
   sa.tile_slow = h->d_tile_slow;
   sa.slow_tiles = h->d_slow_tiles;
   sa.tile_index = h->d_tile_index;
@@ -691,8 +692,9 @@ SweepArgs channel_args(const cflbm_handle *h, const void *fa, void *fb, bool wri
   sa.face_bb = h->d_face_bb;
   sa.links_bits = h->d_links_bits;
   sa.n_slow = h->n_slow;
-  sa.force_tiles = h->d_force_tiles;
-  sa.n_force = h->n_force;
+  sa.bcell_idx = h->d_bcell_idx;
+  sa.bcell_links = h->d_bcell_links;
+  sa.n_bcells = h->n_bcells;
   sa.partials = h->d_partials;
   sa.counter = h->d_counter;
   sa.hist = h->d_hist;

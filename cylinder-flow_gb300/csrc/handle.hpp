@@ -25,8 +25,9 @@ struct cflbm_handle {
   unsigned char *d_tile_slow = nullptr;  // per warp tile: listed (face row or next to a solid)
   int *d_slow_tiles = nullptr;           // list of those tiles
   int *d_tile_index = nullptr;           // per warp tile: position in that list or -1
-  int *d_force_tiles = nullptr;  // list positions of the tiles with force work
-  int n_force = 0;               // its length
+  long long *d_bcell_idx = nullptr;  // boundary cells (fluid, solid links): storage index
+  unsigned *d_bcell_links = nullptr;  // and link word of each, in tile and x order
+  int n_bcells = 0;                   // their number
   long long *d_face_off = nullptr;       // listed-tile pull offsets per face state
   unsigned *d_face_bb = nullptr;         // no-slip face bounce-back bits per face state
   // Channel profile: the steps do not write u, v, w, p; the fields of the last

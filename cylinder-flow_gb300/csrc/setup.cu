@@ -210,40 +210,56 @@ __global__ void tile_list_kernel(const SetupArgs s, const unsigned char *flag,
   }
 }
 
-// One warp per listed tile t: flag[t] = 1 when a fluid cell of the tile has
-// solid links.
-__global__ void force_flags_kernel(int n_slow, const uint32_t *links_bits, unsigned char *flag) {
+// One warp per listed tile t: cnt[t] = its fluid cells with solid links.
+__global__ void bcell_count_kernel(int n_slow, const uint32_t *links_bits, unsigned char *cnt) {
   const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (t >= n_slow) return;  // warp-uniform
   const unsigned word = links_bits[t * 32 + lane];
-  const bool f = __any_sync(0xffffffffu, (word & 0x7fffffffu) != 0u && !(word >> 31));
-  if (lane == 0) flag[t] = f ? 1 : 0;
+  const unsigned b =
+      __ballot_sync(0xffffffffu, (word & 0x7fffffffu) != 0u && !(word >> 31));
+  if (lane == 0) cnt[t] = (unsigned char)__popc(b);
 }
 
-// Per chunk of TILES_PER_CHUNK flags: their count.
-__global__ void flag_count_kernel(int n, const unsigned char *flag, int *chunk) {
+// Per chunk of TILES_PER_CHUNK tiles: the sum of their counts.
+__global__ void bcell_chunk_kernel(int n, const unsigned char *cnt, int *chunk) {
   __shared__ int sh[SETUP_THREADS / 32];
   const long long t0 = (long long)blockIdx.x * TILES_PER_CHUNK + threadIdx.x * TILES_PER_THREAD;
   int c = 0;
   for (int k = 0; k < TILES_PER_THREAD; ++k)
-    if (t0 + k < n) c += flag[t0 + k];
+    if (t0 + k < n) c += cnt[t0 + k];
   int total;
   (void)block_exclusive_sum(c, sh, total);
   if (threadIdx.x == 0) chunk[blockIdx.x] = total;
 }
 
-// Per chunk: the flagged positions at the chunk's offset, in order.
-__global__ void flag_list_kernel(int n, const unsigned char *flag, const int *chunk, int *out) {
+// Per chunk: its tiles' boundary cells at the chunk's offset, in tile and
+// then x order: the storage index and the link word of each.
+__global__ void bcell_list_kernel(const Layout L, int nxw, int n, const int *list,
+                                  const uint32_t *links_bits, const unsigned char *cnt,
+                                  const int *chunk, long long *cell, uint32_t *words) {
   __shared__ int sh[SETUP_THREADS / 32];
   const long long t0 = (long long)blockIdx.x * TILES_PER_CHUNK + threadIdx.x * TILES_PER_THREAD;
   int c = 0;
   for (int k = 0; k < TILES_PER_THREAD; ++k)
-    if (t0 + k < n) c += flag[t0 + k];
+    if (t0 + k < n) c += cnt[t0 + k];
   int total;
   int pos = chunk[blockIdx.x] + block_exclusive_sum(c, sh, total);
-  for (int k = 0; k < TILES_PER_THREAD; ++k)
-    if (t0 + k < n && flag[t0 + k]) out[pos++] = (int)(t0 + k);
+  for (int k = 0; k < TILES_PER_THREAD; ++k) {
+    const long long t = t0 + k;
+    if (t >= n || !cnt[t]) continue;
+    const int tile = list[t];
+    const int row = tile / nxw;
+    const long long c0 = L.idx((tile % nxw) * 32, row % L.ny, row / L.ny);
+    for (int l = 0; l < 32; ++l) {
+      const uint32_t w = links_bits[t * 32 + l];
+      if ((w & 0x7fffffffu) && !(w >> 31)) {
+        cell[pos] = c0 + l;
+        words[pos] = w;
+        ++pos;
+      }
+    }
+  }
 }
 
 int grid_for(long long n) {
@@ -287,22 +303,30 @@ cudaError_t launch_setup_list(const SetupArgs &s, const unsigned char *flag, con
   return cudaGetLastError();
 }
 
-int force_chunks(int n_slow) {
+int bcell_chunks(int n_slow) {
   return std::max(1, (n_slow + TILES_PER_CHUNK - 1) / TILES_PER_CHUNK);
 }
 
-cudaError_t launch_setup_force_list(const SetupArgs &s, int n_slow, const uint32_t *links_bits,
-                                    unsigned char *flag, int *chunk, int *total,
-                                    int *force_list, cudaStream_t st) {
-  (void)s;
-  const int nchunks = force_chunks(n_slow);
+cudaError_t launch_setup_bcell_count(int n_slow, const uint32_t *links_bits, unsigned char *cnt,
+                                     int *chunk, int *total, cudaStream_t st) {
+  const int nchunks = bcell_chunks(n_slow);
   if (n_slow > 0)
-    force_flags_kernel<<<(unsigned)((32LL * n_slow + SETUP_THREADS - 1) / SETUP_THREADS),
-                         SETUP_THREADS, 0, st>>>(n_slow, links_bits, flag);
-  flag_count_kernel<<<nchunks, SETUP_THREADS, 0, st>>>(n_slow, flag, chunk);
+    bcell_count_kernel<<<(unsigned)((32LL * n_slow + SETUP_THREADS - 1) / SETUP_THREADS),
+                         SETUP_THREADS, 0, st>>>(n_slow, links_bits, cnt);
+  bcell_chunk_kernel<<<nchunks, SETUP_THREADS, 0, st>>>(n_slow, cnt, chunk);
   chunk_scan_kernel<<<1, SETUP_THREADS, 0, st>>>(chunk, nchunks, total);
-  flag_list_kernel<<<nchunks, SETUP_THREADS, 0, st>>>(n_slow, flag, chunk, force_list);
-  count_launch(n_slow > 0 ? 4 : 3);
+  count_launch(n_slow > 0 ? 3 : 2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_setup_bcell_list(const Layout &L, int nxw, int n_slow, const int *list,
+                                    const uint32_t *links_bits, const unsigned char *cnt,
+                                    const int *chunk, long long *cell, uint32_t *words,
+                                    cudaStream_t st) {
+  bcell_list_kernel<<<bcell_chunks(n_slow), SETUP_THREADS, 0, st>>>(L, nxw, n_slow, list,
+                                                                   links_bits, cnt, chunk,
+                                                                   cell, words);
+  count_launch();
   return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "solver.cuh"
 
 namespace cflbm {
 
@@ -27,12 +28,16 @@ cudaError_t launch_setup_list(const SetupArgs &s, const unsigned char *flag, con
                               const uint32_t *mask, const uint32_t *bits, int *tile_index,
                               int *list, uint32_t *links_bits, cudaStream_t st);
 
-// The positions in the list of the listed tiles with force work (a fluid cell
-// with solid links), in list (= tile) order; its length into *total.  flag:
-// n_slow bytes; chunk: force_chunks(n_slow) ints.
-int force_chunks(int n_slow);
-cudaError_t launch_setup_force_list(const SetupArgs &s, int n_slow, const uint32_t *links_bits,
-                                    unsigned char *flag, int *chunk, int *total,
-                                    int *force_list, cudaStream_t st);
+// The boundary cells (fluid cells with solid links) of the listed tiles, in
+// tile and then x order, for the force launch: per listed tile its count
+// (cnt: n_slow bytes; chunk: bcell_chunks(n_slow) + 1 ints; their number into
+// *total), then the storage index and link word of each.
+int bcell_chunks(int n_slow);
+cudaError_t launch_setup_bcell_count(int n_slow, const uint32_t *links_bits, unsigned char *cnt,
+                                     int *chunk, int *total, cudaStream_t st);
+cudaError_t launch_setup_bcell_list(const Layout &L, int nxw, int n_slow, const int *list,
+                                    const uint32_t *links_bits, const unsigned char *cnt,
+                                    const int *chunk, long long *cell, uint32_t *words,
+                                    cudaStream_t st);
 
 }  // namespace cflbm

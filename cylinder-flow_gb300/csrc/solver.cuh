@@ -88,8 +88,9 @@ struct SweepArgs {
   const int *slow_tiles; // list of tiles next to solids (tile = (z*ny + y)*nxw + x/32)
   const int *tile_index; // per warp tile: its position in slow_tiles, -1 if not listed
   int n_slow;            // length of the list
-  const int *force_tiles;  // list positions of the tiles with force work (tile order)
-  int n_force;             // its length
+  const long long *bcell_idx;  // boundary cells (fluid, solid links): storage index
+  const unsigned *bcell_links; // and link word of each, in tile and x order
+  int n_bcells;                // their number
   const unsigned *links_bits;  // per listed tile, 32 cells: bit i = source of i is solid,
                                // bit 31 = the cell is solid
   const long long *face_off;   // [16][Q] listed-tile pull offsets per face state
@@ -99,7 +100,7 @@ struct SweepArgs {
   double *hist;          // force history, 3 doubles per step
   long long *step;       // device step counter (history slot = step % cap)
   long long cap;
-  int bnd_blocks;        // grid of the force launch (persistent, about one block per SM)
+  int bnd_blocks;        // grid of the force launch (at most one block per SM)
   int sms;               // multiprocessors of the device
   int lines;             // 1: the interior runs the line-staged sweep (sweep_lines.cuh)
   unsigned *err;         // device error word of the handle (a bounded wait gave up)

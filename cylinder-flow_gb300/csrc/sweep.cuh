@@ -918,7 +918,7 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) sweep_channel_kerne
   finish_cell<L, SF, A, E>(f, rho3, ux, uy, uz, cell, valid, fb, c, S, a);
 }
 
-// Sums per-thread FP64 force partials of a persistent grid: warp shuffles, per
+// Sums per-thread FP64 force partials of a small grid: warp shuffles, per
 // block into partials[blockIdx.x], then over blocks, in block order, by the last
 // block to finish, into the force-history slot of this step.
 __device__ __forceinline__ void force_to_history(const SweepArgs &a, double dx, double dy,
@@ -984,45 +984,38 @@ __device__ __forceinline__ void force_to_history(const SweepArgs &a, double dx, 
   }
 }
 
-// Momentum-exchange force on the solids for this step: a small persistent grid
-// (about one block per SM) on a second stream beside the sweep strides over
-// the listed tiles with force work (fluid cells with solid links; the set-up's
-// list, in tile order) and, for every fluid cell with solid links, reads the
-// populations the sweep bounces back (f*_{opp(I)}(X) from the state it pulls
-// from); per cell the sum runs in the arithmetic type, over cells in FP64.
+// Momentum-exchange force on the solids for this step, beside the sweep on a
+// second stream: a small grid (at most one block per SM) strides over the
+// boundary cells (fluid cells with solid links; the set-up's list, in tile and
+// x order), one cell per thread, and reads the populations the sweep bounces
+// back (f*_{opp(I)}(X) from the state it pulls from); per cell the sum runs in
+// the arithmetic type, over cells in FP64.
 template <int Q, class ST, class A, int MINB>
 __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) channel_force_kernel(const SweepArgs a) {
   using L = Lat<Q>;
   using SF = Store<ST>;
   using E = typename SF::elem;
-  const int nx = a.L.nx, ny = a.L.ny;
-  const int lane = threadIdx.x, wid = threadIdx.y;
   const long long S = a.L.S;
   const E *__restrict__ fa = static_cast<const E *>(a.fa);
+  const long long stride = (long long)gridDim.x * SWEEP_BX * SWEEP_BY;
   double dx = 0.0, dy = 0.0, dz = 0.0;
-  for (long long base = (long long)blockIdx.x * SWEEP_BY; base < a.n_force;
-       base += (long long)gridDim.x * SWEEP_BY) {
-    if (base + wid >= a.n_force) continue;  // warp-uniform
-    const long long t = a.force_tiles[base + wid];
-    const unsigned word = a.links_bits[t * SWEEP_BX + lane];
-    const unsigned links = word & ~(1u << 31);
+  for (long long k = (long long)blockIdx.x * SWEEP_BX * SWEEP_BY + threadIdx.y * SWEEP_BX +
+                     threadIdx.x;
+       k < a.n_bcells; k += stride) {
+    const unsigned links = a.bcell_links[k];
+    const long long c = a.bcell_idx[k];
+    A f[Q];
+    static_for(
+        [&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          f[I] = ((links >> I) & 1u)
+                     ? SF::template load<A, L>(fa + (long long)DirC<Q, I>::opp * S + c,
+                                               a.L.fbase[DirC<Q, I>::opp])
+                     : A(0);
+        },
+        std::make_integer_sequence<int, Q>{});
     A Fx = A(0), Fy = A(0), Fz = A(0);
-    if (links && !(word >> 31)) {  // a fluid cell with solid links (x < nx: bits are 0 past nx)
-      const int tile = a.slow_tiles[t];
-      const int row = tile / a.nxw;
-      const long long c = a.L.idx((tile % a.nxw) * SWEEP_BX + lane, row % ny, row / ny);
-      A f[Q];
-      static_for(
-          [&](auto ic) {
-            constexpr int I = decltype(ic)::value;
-            f[I] = ((links >> I) & 1u)
-                       ? SF::template load<A, L>(fa + (long long)DirC<Q, I>::opp * S + c,
-                                                 a.L.fbase[DirC<Q, I>::opp])
-                       : A(0);
-          },
-          std::make_integer_sequence<int, Q>{});
-      cell_force<Q, A, SF>(f, links, Fx, Fy, Fz);
-    }
+    cell_force<Q, A, SF>(f, links, Fx, Fy, Fz);
     if constexpr (sizeof(A) == 4) {
       dx += f2d_bits(Fx);
       dy += f2d_bits(Fy);
@@ -1033,7 +1026,6 @@ __global__ void __launch_bounds__(SWEEP_BX * SWEEP_BY, MINB) channel_force_kerne
       dz += Fz;
     }
   }
-  (void)nx;
   force_to_history(a, dx, dy, dz);
 }
 
