@@ -635,6 +635,10 @@ void set_relax(SweepArgs &a, int Q, int, double omega) {
   split(kw0, RK_W, RK_LW);
   split(k31, RK_3 + 1, RK_L3);
   split(ka1, RK_A + 1, RK_LA);
+  for (int c = 0; c < NC; ++c) {  // -2 K3 (exact)
+    rk[RK_M3 + c] = -2.0 * rk[RK_3 + c];
+    kf[RK_M3 + c] = -2.0f * kf[RK_3 + c];
+  }
   for (int k = 0; k < RK_N; ++k) {
     a.rk[k] = rk[k];
     a.rkf[k] = kf[k];

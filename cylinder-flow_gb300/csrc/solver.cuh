@@ -53,7 +53,7 @@ __host__ __device__ inline bool mask_solid(const uint32_t *m, int nxw, int ny, i
 
 // Indices of the relaxation constants (their meaning: bgk_relax_v, sweep.cuh).
 constexpr int RK_OMC = 0, RK_W = 1, RK_A = 5, RK_3 = 9, RK_LW = 13, RK_L3 = 14, RK_LA = 15,
-              RK_N = 16;
+              RK_M3 = 16, RK_N = 20;
 
 struct SweepArgs {
   Layout L;
