@@ -322,7 +322,9 @@ def run_gb300(args):
                      "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_cell": info.bytes_per_cell_step,
                      "sweep_us": round(sweep_s * 1e6, 2),
-                     "note": "FP64 arithmetic is bound by GB300's FP64 units, not HBM"},
+                     "note": "FP64 arithmetic is bound by GB300's FP64 units, not HBM: "
+                             "133 FP64 instructions per cell at 85 % FP64-pipe activity "
+                             "(ncu, profiles/sweep_instruction_mix_d3q27.md)"},
         "e2e": {"value": round(e2e_value, 2), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps, "forces_read_back": forces_ok,
                 "create_ms": round(1e3 * (t_created - t0), 2)},
