@@ -185,6 +185,22 @@ def test_channel_fp64_matches_oracle(cuda, name):
     assert rel_err(r["force"], o["force"]) < 1e-9, name
 
 
+@pytest.mark.parametrize("name", ["d2q9_cyl_freeslip", "d3q27_cyl", "d3q27_sphere"])
+def test_channel_fp64_stays_at_roundoff(cuda, name):
+    """Over a few steps FP64 arithmetic stays at round-off from the oracle: the
+    moments' cascade and the relaxation's Horner form per +/- pair change only
+    the order of FP64 operations.  One step's arithmetic in FP32 would show at
+    ~1e-7."""
+    case = CHANNEL_CASES[name]
+    o = oracle_channel(case, 5)
+    r = gpu_channel(case, 5)
+    for k in ("u", "v", "w", "p", "fpost"):
+        if k == "w" and case["lattice"] == 9:
+            continue
+        assert rel_err(r[k], o[k]) < 1e-12, (name, k)
+    assert rel_err(r["force"], o["force"]) < 1e-12, name
+
+
 @pytest.mark.parametrize("name", sorted(CHANNEL_CASES))
 def test_channel_df64_matches_oracle(cuda, name):
     """Double-float collision (pairs of FP32, about 48 bits) on FP64 storage stays
